@@ -1,0 +1,506 @@
+"""CPU oracle for the spatial-filtering hot path.
+
+TEST INFRASTRUCTURE ONLY.  This module is the checker: only ``tests/``,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may import
+it.  The product path (the CUDA kernels behind ``include/sf_capi.h``) never
+calls into it and fails loudly when its extension is missing.
+
+It restates, in plain numpy (int64 for the integer work, float64/complex128 for
+the floating-point work), the reference's per-channel chain:
+
+  ingest + alignment   include/spatial/spatial.cuh:423-486 (scale_and_convert),
+                       include/spatial/spatial.cuh:1420-1506 (apply_delays),
+                       include/spatial/pipeline/lambda_corr_beam_only_gpu_pipeline.hpp:305-316
+                       (packet_to_corr_input: packets 0..P-1, no delay)
+  correlation          TCC launch, include/spatial/pipeline/lambda_gpu_pipeline.hpp:649-651;
+                       packed triangle baseline(i,j)=j(j+1)/2+i, i<=j
+                       (tests/support/assertions.hpp:35-37); the value convention
+                       V(i,p;j,q)=sum_t x_ip conj(x_jq) follows tests/test_beamforming.cpp:49-79
+  trim                 src/spatial.cu:176-200 (keep baselines a < R(R+1)/2)
+  unpack               include/spatial/spatial.cuh:672-713 (upper triangle, column-major)
+  whitening            include/spatial/spatial.cuh:1068-1148
+  eigendecomposition   cusolverDnXsyevBatched (ascending, vectors in columns); restated
+                       here with LAPACK (numpy.linalg.eigh) in complex128
+  K detection          include/spatial/spatial.cuh:900-950 (float32 arithmetic) and
+                       scripts/adaptive_detection_reference.py:11-35 (float64)
+  projector            include/spatial/spatial.cuh:993-1034 (P = I - U_K U_K^H),
+                       shrink form spatial.cuh:952-1063 / adaptive_detection_reference.py:50-63
+  weight projection    lambda_adaptive_beamformed_spectra_pipeline.hpp:773-794 (W' = W P)
+  beamforming          lambda_gpu_pipeline.hpp:731-733 (Y = W X, no conjugation)
+  half output          include/spatial/spatial.cuh:376-418
+
+Gains and fine-delay phasors are folded as a per-(channel, pol, receiver)
+complex factor d: the covariance becomes d_i conj(d_j) V and the beam weights
+become W diag(d).  This equals the reference's ingest (which multiplies each
+sample by its gain before correlating and beamforming) up to the reference's
+fp16 rounding of the scaled sample.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+COMPLEX = 2
+NPOL = 2
+
+
+# --------------------------------------------------------------------------
+# Shapes and index helpers
+# --------------------------------------------------------------------------
+class Shape:
+    """Runtime shape of one integration (the reference's LambdaConfig,
+    include/spatial/packet_formats.hpp:265-407)."""
+
+    def __init__(self, n_channels, n_fpgas, n_time_per_packet, n_receivers,
+                 n_receivers_per_packet, n_packets, n_beams, n_pol=2):
+        if n_pol != 2:
+            raise ValueError("only 2 polarisations are supported")
+        if n_receivers != n_fpgas * n_receivers_per_packet:
+            raise ValueError("n_receivers must equal n_fpgas * n_receivers_per_packet")
+        self.C = int(n_channels)
+        self.F = int(n_fpgas)
+        self.Tp = int(n_time_per_packet)
+        self.R = int(n_receivers)
+        self.Rpp = int(n_receivers_per_packet)
+        self.P = int(n_packets)
+        self.B = int(n_beams)
+        self.T = self.P * self.Tp
+        self.NBL = self.R * (self.R + 1) // 2
+
+    def samples_shape(self):
+        return (self.C, self.P + 2, self.F, self.Tp, self.Rpp, NPOL, COMPLEX)
+
+    def scales_shape(self):
+        return (self.C, self.P + 2, self.R, NPOL)
+
+
+def baseline_index(i, j):
+    """Packed index of baseline (i, j), i <= j (tests/support/assertions.hpp:35-37)."""
+    return j * (j + 1) // 2 + i
+
+
+def baseline_pairs(R):
+    """(i, j) arrays in packed order."""
+    ii, jj = [], []
+    for j in range(R):
+        for i in range(j + 1):
+            ii.append(i)
+            jj.append(j)
+    return np.array(ii), np.array(jj)
+
+
+# --------------------------------------------------------------------------
+# Ingest: packet layout -> aligned, scaled integer samples
+# --------------------------------------------------------------------------
+def sample_offsets(shape, delays=None, mode="aligned"):
+    """Per-FPGA offset (in samples) of the integration window inside the
+    (P+2)-packet buffer.
+
+    mode "aligned": the LambdaGPUPipeline/adaptive path; window starts one
+        packet in, shifted by the sub-packet delay (spatial.cuh:1436-1442).
+    mode "packet": the LambdaCorrBeamOnlyGPUPipeline path; window is packets
+        0..P-1 with no delay (spatial.cuh:215-279).
+    """
+    if mode == "packet":
+        return np.zeros(shape.F, dtype=np.int64)
+    d = np.zeros(shape.F, dtype=np.int64) if delays is None else np.asarray(delays, np.int64)
+    if np.any(np.abs(d) > shape.Tp):
+        raise ValueError("sub-packet delays must lie in [-Tp, Tp]")
+    return shape.Tp + d
+
+
+def aligned_samples(shape, samples, scales, offsets):
+    """Scaled integer samples x[c][p][r][t] (re, im as int64 arrays).
+
+    x = int(sample) * int(scale), as scale_and_convert_to_half_kernel
+    (spatial.cuh:464-476) computes before its float conversion.
+    """
+    s = np.asarray(samples).reshape(shape.samples_shape()).astype(np.int64)
+    sc = np.asarray(scales).reshape(shape.scales_shape()).astype(np.int64)
+    re = np.zeros((shape.C, NPOL, shape.R, shape.T), dtype=np.int64)
+    im = np.zeros_like(re)
+    t_al = np.arange(shape.T)
+    for f in range(shape.F):
+        q = t_al + int(offsets[f])
+        pkt = q // shape.Tp
+        tin = q % shape.Tp
+        # [C][T][Rpp][Pol][2]
+        blk = s[:, pkt, f, tin, :, :, :]
+        scl = sc[:, pkt, f * shape.Rpp:(f + 1) * shape.Rpp, :]  # [C][T][Rpp][Pol]
+        r0 = f * shape.Rpp
+        re[:, :, r0:r0 + shape.Rpp, :] = np.transpose(blk[..., 0] * scl, (0, 3, 2, 1))
+        im[:, :, r0:r0 + shape.Rpp, :] = np.transpose(blk[..., 1] * scl, (0, 3, 2, 1))
+    return re, im
+
+
+# --------------------------------------------------------------------------
+# Correlation (exact integers)
+# --------------------------------------------------------------------------
+def correlate(shape, re, im):
+    """Exact visibilities vis[c][b][p][q][2] (int64), b = baseline(i, j), i <= j,
+    value sum_t x_{i,p}(t) conj(x_{j,q}(t))."""
+    C, R = shape.C, shape.R
+    ii, jj = baseline_pairs(R)
+    out = np.zeros((C, shape.NBL, NPOL, NPOL, COMPLEX), dtype=np.int64)
+    for c in range(C):
+        a = re[c].reshape(NPOL * R, shape.T)  # rows (p, r)
+        b = im[c].reshape(NPOL * R, shape.T)
+        rr = a @ a.T + b @ b.T               # Re sum x_u conj(x_v)
+        ri = b @ a.T - a @ b.T               # Im
+        rr = rr.reshape(NPOL, R, NPOL, R)
+        ri = ri.reshape(NPOL, R, NPOL, R)
+        # out[c, bl, p, q] = V(i,p ; j,q)
+        # advanced indexing puts the baseline axis first: [b][p][q]
+        out[c, :, :, :, 0] = rr[:, ii, :, jj]
+        out[c, :, :, :, 1] = ri[:, ii, :, jj]
+    return out
+
+
+def vis_complex(vis):
+    v = np.asarray(vis)
+    return v[..., 0].astype(np.float64) + 1j * v[..., 1].astype(np.float64)
+
+
+# --------------------------------------------------------------------------
+# Per-receiver complex factors (gains x fine-delay phasors)
+# --------------------------------------------------------------------------
+def fine_delay_phasors(shape, delays_ns, base_freq_hz, channel_bw_hz, min_freq_ch):
+    """Channel-centre phasor exp(-2 pi i f_c tau_r), f_c = base + (min_ch + c) bw.
+
+    The reference corrects every fine bin k with f_fine = f_c + (k_signed/N) bw
+    (lambda_gpu_pipeline.hpp:1100-1131); folding the channel-centre phasor into
+    the weights is the narrowband approximation (exact for the k = 0 bin).
+    """
+    tau = np.asarray(delays_ns, np.float64) * 1e-9
+    fc = base_freq_hz + (min_freq_ch + np.arange(shape.C, dtype=np.float64)) * channel_bw_hz
+    phi = -2.0 * np.pi * fc[:, None] * tau[None, :]
+    return np.exp(1j * phi)  # [C][R]
+
+
+def receiver_factors(shape, gains=None, phasors=None):
+    """d[c][p][r] complex128; gains [C][Pol][R] complex (AntennaGains layout,
+    packet_formats.hpp:387-390), phasors [C][R]."""
+    d = np.ones((shape.C, NPOL, shape.R), dtype=np.complex128)
+    if gains is not None:
+        d = d * np.asarray(gains, np.complex128).reshape(shape.C, NPOL, shape.R)
+    if phasors is not None:
+        d = d * np.asarray(phasors, np.complex128).reshape(shape.C, 1, shape.R)
+    return d
+
+
+def scaled_visibilities(shape, vis, d):
+    """Float visibilities as the reference reports them: d_{i,p} conj(d_{j,q}) V."""
+    ii, jj = baseline_pairs(shape.R)
+    v = vis_complex(vis)
+    di = np.transpose(d[:, :, ii], (0, 2, 1))  # [C][NBL][Pol]
+    dj = np.transpose(d[:, :, jj], (0, 2, 1))
+    return v * di[:, :, :, None] * np.conj(dj[:, :, None, :])
+
+
+# --------------------------------------------------------------------------
+# Covariance matrices
+# --------------------------------------------------------------------------
+def unpack_hermitian(shape, vis_c, p, q):
+    """Dense Hermitian matrices [C][R][R] built the way cuSOLVER reads the
+    reference's unpack output (spatial.cuh:672-713 writes the upper triangle
+    row=i, col=j, i<=j; uplo=UPPER; the diagonal's imaginary part is ignored)."""
+    ii, jj = baseline_pairs(shape.R)
+    C, R = shape.C, shape.R
+    m = np.zeros((C, R, R), dtype=np.complex128)
+    m[:, ii, jj] = vis_c[:, :, p, q]
+    lower = np.conj(np.transpose(m, (0, 2, 1)))
+    m = m + lower
+    diag = np.arange(R)
+    m[:, diag, diag] = np.real(vis_c[:, baseline_index(diag, diag), p, q])
+    return m
+
+
+def whiten(m):
+    """spatial.cuh:1068-1093: s_i = sqrt(max(Re m_ii, 1e-10)); m_ij / (s_i s_j)."""
+    dg = np.real(np.diagonal(m, axis1=-2, axis2=-1))
+    s = np.sqrt(np.maximum(dg, 1e-10))
+    return m / (s[..., :, None] * s[..., None, :]), s
+
+
+def unwhiten_normalize(v, s):
+    """spatial.cuh:1098-1126: u_ik = s_i v_ik, then each column to unit norm."""
+    u = v * s[..., :, None]
+    nrm = np.sqrt(np.sum(np.abs(u) ** 2, axis=-2, keepdims=True))
+    inv = np.where(nrm > 0, 1.0 / np.where(nrm > 0, nrm, 1.0), 0.0)
+    return u * inv
+
+
+def eigh_ascending(m):
+    """FP64 LAPACK eigendecomposition: ascending eigenvalues, vectors in columns."""
+    w, v = np.linalg.eigh(m)
+    return w, v
+
+
+def normalize_phase(v):
+    """Make each column's largest-magnitude component real and positive (ties:
+    lowest index).  Eigenvectors are unique only up to a unit phase; this is
+    the convention the CUDA eigensolver applies to its output."""
+    v = np.array(v, dtype=np.complex128, copy=True)
+    mag = np.abs(v)
+    idx = np.argmax(mag, axis=-2)  # [..., k]
+    piv = np.take_along_axis(v, idx[..., None, :], axis=-2)
+    ph = np.where(np.abs(piv) > 0, np.conj(piv) / np.where(np.abs(piv) > 0, np.abs(piv), 1.0), 1.0)
+    return v * ph
+
+
+# --------------------------------------------------------------------------
+# K detection
+# --------------------------------------------------------------------------
+def _percentile_f32(vals, quant):
+    n = len(vals)
+    if n <= 0:
+        return np.float32(0.0)
+    if n == 1:
+        return np.float32(vals[0])
+    q = np.float32(min(1.0, max(0.0, quant)))
+    pos = np.float32(q * np.float32(n - 1))
+    lo = int(np.floor(pos))
+    hi = int(np.ceil(pos))
+    if lo == hi:
+        return np.float32(vals[lo])
+    frac = np.float32(pos - np.float32(lo))
+    return np.float32(vals[lo] + frac * np.float32(vals[hi] - vals[lo]))
+
+
+def detect_k_f32(evals, delta):
+    """detectSignalEigenmodeCountsKernel (spatial.cuh:900-943), float32."""
+    e = np.asarray(evals, dtype=np.float32)
+    p20 = _percentile_f32(e, 0.2)
+    p50 = _percentile_f32(e, 0.5)
+    p80 = _percentile_f32(e, 0.8)
+    sigma = np.float32(np.float32(p80 - p20) / np.float32(2.0 * 0.8416))
+    thr = np.float32(p50 + np.float32(delta) * sigma)
+    return int(np.count_nonzero(e > thr))
+
+
+def detect_k_f64(evals, delta):
+    """scripts/adaptive_detection_reference.py:28-35, float64."""
+    e = np.asarray(evals, dtype=np.float64)
+
+    def pct(q):
+        n = e.size
+        if n == 0:
+            return 0.0
+        if n == 1:
+            return float(e[0])
+        pos = float(np.clip(q, 0.0, 1.0)) * (n - 1)
+        lo, hi = int(np.floor(pos)), int(np.ceil(pos))
+        if lo == hi:
+            return float(e[lo])
+        return float(e[lo] + (pos - lo) * (e[hi] - e[lo]))
+
+    sigma = (pct(0.8) - pct(0.2)) / (2.0 * 0.8416)
+    thr = pct(0.5) + delta * sigma
+    return int(np.count_nonzero(e > thr))
+
+
+def detect_k_noise_floor(evals, factor=10.0, floor=None):
+    """K = #{lambda > factor x noise floor}; the noise floor defaults to the
+    median eigenvalue (the uneven-batching configuration's rule)."""
+    e = np.asarray(evals, dtype=np.float64)
+    nf = float(np.median(e)) if floor is None else float(floor)
+    return int(np.count_nonzero(e > factor * nf))
+
+
+# --------------------------------------------------------------------------
+# Projectors and weights
+# --------------------------------------------------------------------------
+def null_projection(u, k):
+    """P = I - U_K U_K^H over the last k columns (spatial.cuh:993-1022)."""
+    n = u.shape[-1]
+    eye = np.eye(n, dtype=np.complex128)
+    if k <= 0:
+        return eye
+    rfi = u[:, n - k:]
+    return eye - rfi @ np.conj(rfi.T)
+
+
+def shrink_projection(v, evals, k):
+    """M = V diag(d) V^H, d = 1 for kept modes, lambda_bar/lambda for the last k
+    (spatial.cuh:952-984, adaptive_detection_reference.py:50-63)."""
+    vals = np.asarray(evals, np.float64)
+    n = vals.shape[0]
+    d = np.ones(n)
+    kk = max(0, min(n, int(k)))
+    if kk > 0:
+        keep = n - kk
+        lam_bar = float(np.mean(vals[:keep])) if keep > 0 else 0.0
+        for idx in range(keep, n):
+            d[idx] = lam_bar / vals[idx] if vals[idx] > 0.0 else 0.0
+    return (v * d[None, :]) @ np.conj(v.T)
+
+
+def weights_complex(weights):
+    """BeamWeightsT layout complex<__half>[C][Pol][B][R] (pipeline/common.hpp:52-55)
+    given as float pairs [..., 2] or complex."""
+    w = np.asarray(weights)
+    if np.iscomplexobj(w):
+        return w.astype(np.complex128)
+    return w[..., 0].astype(np.float64) + 1j * w[..., 1].astype(np.float64)
+
+
+# --------------------------------------------------------------------------
+# Beamforming
+# --------------------------------------------------------------------------
+def beamform(shape, re, im, w_eff):
+    """Y[c][p][m][t] = sum_r W_eff[c][p][m][r] x[c][p][r][t] (no conjugation)."""
+    x = re.astype(np.float64) + 1j * im.astype(np.float64)
+    return np.einsum("cpmr,cprt->cpmt", w_eff, x)
+
+
+def half_output(y):
+    """__half[C][Pol][NB][T][2] as beam_ccglib_to_half_output writes it
+    (spatial.cuh:376-404): round-to-nearest fp16 of each component."""
+    out = np.empty(y.shape + (2,), dtype=np.float16)
+    out[..., 0] = np.real(y).astype(np.float32).astype(np.float16)
+    out[..., 1] = np.imag(y).astype(np.float32).astype(np.float16)
+    return out
+
+
+# --------------------------------------------------------------------------
+# Whole chains
+# --------------------------------------------------------------------------
+def corr_beam_chain(shape, samples, scales, weights, d=None, offsets=None):
+    """LambdaCorrBeamOnlyGPUPipeline (lambda_corr_beam_only_gpu_pipeline.hpp:305-344):
+    exact visibilities + beams with the unprojected weights."""
+    if offsets is None:
+        offsets = sample_offsets(shape, mode="packet")
+    if d is None:
+        d = receiver_factors(shape)
+    re, im = aligned_samples(shape, samples, scales, offsets)
+    vis = correlate(shape, re, im)
+    w = weights_complex(weights) * d[:, :, None, :]
+    y = beamform(shape, re, im, w)
+    return {"vis": vis, "beams": y, "re": re, "im": im}
+
+
+def lambda_gpu_chain(shape, samples, scales, weights, delays=None, d=None):
+    """LambdaGPUPipeline (lambda_gpu_pipeline.hpp:445-743): aligned window,
+    eigendecomposition of all C*Pol*Pol blocks, beams with unprojected weights."""
+    offsets = sample_offsets(shape, delays, mode="aligned")
+    if d is None:
+        d = receiver_factors(shape)
+    re, im = aligned_samples(shape, samples, scales, offsets)
+    vis = correlate(shape, re, im)
+    vc = scaled_visibilities(shape, vis, d)
+    evals = np.zeros((shape.C, NPOL, NPOL, shape.R))
+    evecs = np.zeros((shape.C, NPOL, NPOL, shape.R, shape.R), dtype=np.complex128)
+    for p in range(NPOL):
+        for q in range(NPOL):
+            m = unpack_hermitian(shape, vc, p, q)
+            for c in range(shape.C):
+                w, v = eigh_ascending(m[c])
+                evals[c, p, q] = w
+                evecs[c, p, q] = normalize_phase(v).T  # [k][l] = component l of vector k
+    w = weights_complex(weights) * d[:, :, None, :]
+    y = beamform(shape, re, im, w)
+    return {"vis": vis, "vis_scaled": vc, "evals": evals, "evecs": evecs,
+            "beams": y, "re": re, "im": im}
+
+
+def adaptive_chain(shape, samples, scales, weights, k_fixed=None, detect=False,
+                   delta=3.0, shrink=False, delays=None, d=None, k_rule=None):
+    """Adaptive null/shrink chain
+    (lambda_adaptive_beamformed_spectra_pipeline.hpp:563-798): per (c, p)
+    same-polarisation covariance, diagonal whitening, eigendecomposition, K,
+    un-whitened I - U U^H (or shrink V diag(d) V^H), W' = W P; beams for the
+    original (slot 0) and projected (slot 1) weights."""
+    offsets = sample_offsets(shape, delays, mode="aligned")
+    if d is None:
+        d = receiver_factors(shape)
+    re, im = aligned_samples(shape, samples, scales, offsets)
+    vis = correlate(shape, re, im)
+    vc = scaled_visibilities(shape, vis, d)
+    C, R, B = shape.C, shape.R, shape.B
+    evals = np.zeros((C, NPOL, R))
+    evecs = np.zeros((C, NPOL, R, R), dtype=np.complex128)
+    counts = np.zeros((C, NPOL), dtype=np.int32)
+    proj = np.zeros((C, NPOL, R, R), dtype=np.complex128)
+    wc = weights_complex(weights)
+    w_eff = np.zeros((C, NPOL, 2 * B, R), dtype=np.complex128)
+    for p in range(NPOL):
+        m = unpack_hermitian(shape, vc, p, p)
+        for c in range(C):
+            mw, s = whiten(m[c])
+            lam, v = eigh_ascending(mw)
+            if k_rule is not None:
+                k = int(k_rule(lam))
+            elif detect:
+                k = detect_k_f32(lam, delta)
+            else:
+                k = 0 if k_fixed is None else int(np.asarray(k_fixed).reshape(C)[c])
+            k = max(0, min(R, k))
+            if shrink:
+                pm = shrink_projection(v, lam, k)
+                vout = v
+            else:
+                u = unwhiten_normalize(v, s)
+                pm = null_projection(u, k)
+                vout = u
+            evals[c, p] = lam
+            evecs[c, p] = normalize_phase(vout).T
+            counts[c, p] = k
+            proj[c, p] = pm
+            w_eff[c, p, :B] = wc[c, p] * d[c, p][None, :]
+            w_eff[c, p, B:] = (wc[c, p] @ pm) * d[c, p][None, :]
+    y = beamform(shape, re, im, w_eff)
+    return {"vis": vis, "vis_scaled": vc, "evals": evals, "evecs": evecs,
+            "counts": counts, "proj": proj, "w_eff": w_eff, "beams": y,
+            "re": re, "im": im}
+
+
+# --------------------------------------------------------------------------
+# Synthetic LAMBDA-shaped inputs (seeded)
+# --------------------------------------------------------------------------
+def synth_inputs(shape, seed=0, sigma=16.0, n_interferers=0, inr_db=20.0,
+                 frac_channels=0.1, scale_value=1):
+    """Seeded synthetic integration in the packet layout.
+
+    Noise: I, Q = clip(round(N(0, sigma^2)), -127, 127).  Interferers (in a
+    random `frac_channels` of the channels) add sqrt(INR * 2 sigma^2) s(t) a
+    with unit-norm random complex steering a and unit-power narrowband s(t);
+    INR is the interferer eigenvalue over the per-receiver noise eigenvalue.
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    C, R, T = shape.C, shape.R, shape.T
+    npk = shape.P + 2
+    tt = npk * shape.Tp
+    re = rng.normal(0.0, sigma, size=(C, tt, R, NPOL))
+    im = rng.normal(0.0, sigma, size=(C, tt, R, NPOL))
+    rfi_ch = np.zeros(C, dtype=bool)
+    if n_interferers > 0:
+        nsel = max(1, int(round(frac_channels * C)))
+        rfi_ch[rng.choice(C, size=nsel, replace=False)] = True
+        amp = np.sqrt(10.0 ** (inr_db / 10.0) * 2.0 * sigma ** 2)
+        t = np.arange(tt)
+        for c in np.nonzero(rfi_ch)[0]:
+            for _ in range(n_interferers):
+                a = rng.normal(size=(R, NPOL)) + 1j * rng.normal(size=(R, NPOL))
+                a /= np.linalg.norm(a, axis=0, keepdims=True)
+                f0 = rng.uniform(-0.45, 0.45)
+                ph0 = rng.uniform(0, 2 * np.pi)
+                s = np.exp(1j * (2 * np.pi * f0 * t + ph0))
+                sig = amp * s[:, None, None] * a[None, :, :]
+                re[c] += np.real(sig)
+                im[c] += np.imag(sig)
+    re = np.clip(np.round(re), -127, 127).astype(np.int8)
+    im = np.clip(np.round(im), -127, 127).astype(np.int8)
+    # [C][tt][R][Pol] -> [C][P+2][F][Tp][Rpp][Pol][2]
+    x = np.stack([re, im], axis=-1).reshape(C, npk, shape.Tp, shape.F, shape.Rpp, NPOL, 2)
+    samples = np.ascontiguousarray(np.transpose(x, (0, 1, 3, 2, 4, 5, 6)))
+    scales = np.full(shape.scales_shape(), scale_value, dtype=np.int16)
+    return samples, scales, rfi_ch
+
+
+def synth_weights(shape, seed=1, n_beams=None):
+    """Unit-modulus weights with uniform random phase, as fp16 pairs
+    [C][Pol][B][R][2] (the BeamWeightsT payload)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    B = shape.B if n_beams is None else n_beams
+    ph = rng.uniform(0, 2 * np.pi, size=(shape.C, NPOL, B, shape.R))
+    w = np.stack([np.cos(ph), np.sin(ph)], axis=-1).astype(np.float16)
+    return w
