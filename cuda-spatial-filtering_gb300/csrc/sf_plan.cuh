@@ -1,0 +1,56 @@
+// Internal plan state shared by the C-ABI translation units.
+#pragma once
+
+#include <cstdint>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "../../include/sf_capi.h"
+
+struct sf_plan {
+  sf_shape shape;
+  int C, F, Tp, R, Rpp, P, B, T, NBL;
+  int device;
+  int num_sms;
+
+  // Window offsets (samples into the (P+2)-packet buffer), one per FPGA.
+  int32_t *d_off_aligned;  // Tp + sub-packet delay
+  int32_t *d_off_packet;   // all zero
+  int32_t *h_delays;       // host copy of the delays
+
+  // Per-(channel, pol, receiver) complex factor d = gain x fine-delay phasor.
+  float2 *d_factors;   // [C][2][R]
+  float2 *h_gains;     // [C][2][R]
+  float2 *h_phasors;   // [C][R]
+  float2 *h_factors;   // [C][2][R] staging for the upload
+
+  __half2 *d_weights;  // [C][2][B][R]
+  float2 *d_weff;      // [C][2][2B][R] effective weights for the beamformer
+  int32_t *d_fixed_counts;  // [C]
+  int32_t *h_fixed_counts;  // [C]
+
+  // Scratch for the whole-chain entry points.
+  int32_t *d_vis;      // [C][NBL][2][2][2]
+  float *d_evals;      // [C][2][2][R]
+  int32_t *d_counts;   // [C][2]
+  uint32_t *d_status;  // error bits
+};
+
+// Launchers (one per translation unit); each returns a cudaError_t.
+cudaError_t sf_launch_correlate(const sf_plan *p, const int8_t *samples, const int16_t *scales,
+                                const int32_t *offsets, int32_t *vis, cudaStream_t stream);
+int sf_correlate_supported(const sf_plan *p, char *why, size_t why_len);
+
+cudaError_t sf_launch_eig(const sf_plan *p, const int32_t *vis, int eig_mode, int k_rule,
+                          float delta, int shrink, float *evals, float2 *evecs, int32_t *counts,
+                          __half2 *proj, cudaStream_t stream);
+int sf_eig_supported(const sf_plan *p, char *why, size_t why_len);
+
+cudaError_t sf_launch_weights_plain(const sf_plan *p, cudaStream_t stream);
+cudaError_t sf_launch_beam(const sf_plan *p, const int8_t *samples, const int16_t *scales,
+                           const int32_t *offsets, int n_slots, __half2 *beams,
+                           cudaStream_t stream);
+cudaError_t sf_launch_vis_accumulate(const sf_plan *p, const int32_t *vis, int64_t *accum,
+                                     cudaStream_t stream);
+cudaError_t sf_launch_vis_to_float(const sf_plan *p, const int64_t *accum, float *out,
+                                   cudaStream_t stream);

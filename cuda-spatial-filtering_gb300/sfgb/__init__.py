@@ -1,0 +1,230 @@
+"""Python host side of the GB300 spatial-filtering hot path.
+
+Thin ctypes binding of ``include/sf_capi.h`` plus Python mirrors of the
+reference's GPU stage interface (``GPUPipeline``,
+include/spatial/pipeline_base.hpp:9-40): ``execute_pipeline`` /
+``dump_visibilities`` / ``set_subpacket_delays`` / ``set_antenna_gains`` /
+``set_fine_delays`` over host packet buffers, writing into an ``Output``
+object with the reference's output layouts.  PyTorch only supplies device
+memory and streams; every computation runs in the sm_103a kernels of
+``libsfgb.so``.  There is no CPU fallback: without the library (or without an
+sm_103 GPU) every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libsfgb.so"
+HEADER = PKG.parent.parent / "include" / "sf_capi.h"
+
+SF_OK = 0
+SF_WINDOW_PACKET = 0
+SF_WINDOW_ALIGNED = 1
+SF_EIG_ALL_BLOCKS = 0
+SF_EIG_SAME_POL_WHITENED = 1
+SF_K_FIXED = 0
+SF_K_DETECT = 1
+SF_K_NOISE_FLOOR = 2
+
+
+class SfError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"sf error {code}: {msg}")
+        self.code = code
+
+
+class ShapeStruct(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in (
+        "n_channels", "n_fpgas", "n_time_per_packet", "n_receivers",
+        "n_polarizations", "n_receivers_per_packet", "n_packets", "n_beams")]
+
+
+_lib = None
+
+_P = ctypes.c_void_p
+_I32 = ctypes.c_int32
+_SIGS = {
+    "sf_plan_create": ([ctypes.POINTER(ShapeStruct), ctypes.POINTER(_P)], ctypes.c_int),
+    "sf_plan_destroy": ([_P], ctypes.c_int),
+    "sf_plan_get_shape": ([_P, ctypes.POINTER(ShapeStruct)], ctypes.c_int),
+    "sf_last_error": ([], ctypes.c_char_p),
+    "sf_plan_status": ([_P, _P, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
+    "sf_set_subpacket_delays": ([_P, _P, _P], ctypes.c_int),
+    "sf_set_antenna_gains": ([_P, _P, _P], ctypes.c_int),
+    "sf_set_fine_delays": ([_P, _P, ctypes.c_double, ctypes.c_double, _I32, _P], ctypes.c_int),
+    "sf_set_weights": ([_P, _P, _P], ctypes.c_int),
+    "sf_set_fixed_counts": ([_P, _P, _P], ctypes.c_int),
+    "sf_correlate": ([_P, _P, _P, _I32, _P, _P], ctypes.c_int),
+    "sf_covariance_eig": ([_P, _P, _I32, _I32, ctypes.c_float, _I32, _P, _P, _P, _P, _P], ctypes.c_int),
+    "sf_beamform": ([_P, _P, _P, _I32, _I32, _P, _P], ctypes.c_int),
+    "sf_accumulate_visibilities": ([_P, _P, _P, _P], ctypes.c_int),
+    "sf_visibilities_to_float": ([_P, _P, _P, _P], ctypes.c_int),
+    "sf_run_corr_beam": ([_P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "sf_run_lambda_gpu": ([_P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "sf_run_adaptive": ([_P, _P, _P, _I32, ctypes.c_float, _I32, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+}
+
+
+def header_symbols():
+    """Function names declared in include/sf_capi.h."""
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(sf_\w+)\s*\(", text, re.M)))
+
+
+def lib():
+    """Load libsfgb.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        L = ctypes.CDLL(str(LIB_PATH))
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != SF_OK:
+        raise SfError(rc, lib().sf_last_error().decode())
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+class Plan:
+    """Owns one sf_plan (device state for one integration shape)."""
+
+    def __init__(self, n_channels, n_fpgas, n_time_per_packet, n_receivers,
+                 n_receivers_per_packet, n_packets, n_beams):
+        import torch
+        if not torch.cuda.is_available():
+            raise RuntimeError("no CUDA device: the spatial-filtering kernels need an sm_103 GPU")
+        self.C, self.F, self.Tp = n_channels, n_fpgas, n_time_per_packet
+        self.R, self.Rpp, self.P, self.B = n_receivers, n_receivers_per_packet, n_packets, n_beams
+        self.T = self.P * self.Tp
+        self.NBL = self.R * (self.R + 1) // 2
+        shape = ShapeStruct(n_channels, n_fpgas, n_time_per_packet, n_receivers, 2,
+                            n_receivers_per_packet, n_packets, n_beams)
+        h = ctypes.c_void_p()
+        _check(lib().sf_plan_create(ctypes.byref(shape), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sf_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- shapes ----
+    def samples_shape(self):
+        return (self.C, self.P + 2, self.F, self.Tp, self.Rpp, 2, 2)
+
+    def scales_shape(self):
+        return (self.C, self.P + 2, self.R, 2)
+
+    def vis_shape(self):
+        return (self.C, self.NBL, 2, 2, 2)
+
+    def beams_shape(self, n_slots=1):
+        return (self.C, 2, n_slots * self.B, self.T, 2)
+
+    # ---- configuration ----
+    def set_subpacket_delays(self, delays=None, stream=None):
+        arr = None if delays is None else np.ascontiguousarray(delays, dtype=np.int32)
+        _check(lib().sf_set_subpacket_delays(self._h, None if arr is None else arr.ctypes.data_as(_P),
+                                             _stream(stream)))
+
+    def set_antenna_gains(self, gains=None, stream=None):
+        arr = None
+        if gains is not None:
+            g = np.asarray(gains).reshape(self.C, 2, self.R)
+            arr = np.ascontiguousarray(np.stack([g.real, g.imag], axis=-1).astype(np.float32))
+        _check(lib().sf_set_antenna_gains(self._h, None if arr is None else arr.ctypes.data_as(_P),
+                                          _stream(stream)))
+
+    def set_fine_delays(self, delays_ns, base_freq_hz, channel_bw_hz, min_freq_ch, stream=None):
+        arr = np.ascontiguousarray(delays_ns, dtype=np.float32)
+        _check(lib().sf_set_fine_delays(self._h, arr.ctypes.data_as(_P), float(base_freq_hz),
+                                        float(channel_bw_hz), int(min_freq_ch), _stream(stream)))
+
+    def set_weights(self, weights_f16, stream=None):
+        arr = np.ascontiguousarray(weights_f16, dtype=np.float16).reshape(self.C, 2, self.B, self.R, 2)
+        _check(lib().sf_set_weights(self._h, arr.ctypes.data_as(_P), _stream(stream)))
+
+    def set_fixed_counts(self, counts=None, stream=None):
+        arr = None if counts is None else np.ascontiguousarray(counts, dtype=np.int32)
+        _check(lib().sf_set_fixed_counts(self._h, None if arr is None else arr.ctypes.data_as(_P),
+                                         _stream(stream)))
+
+    def status(self, stream=None):
+        bits = ctypes.c_uint32(0)
+        rc = lib().sf_plan_status(self._h, _stream(stream), ctypes.byref(bits))
+        return rc, bits.value
+
+    # ---- stages (device tensors) ----
+    def correlate(self, samples, scales, window, vis, stream=None):
+        _check(lib().sf_correlate(self._h, _ptr(samples), _ptr(scales), int(window), _ptr(vis),
+                                  _stream(stream)))
+
+    def covariance_eig(self, vis, eig_mode, k_rule=SF_K_FIXED, delta=0.0, shrink=False, evals=None,
+                       evecs=None, counts=None, proj=None, stream=None):
+        _check(lib().sf_covariance_eig(self._h, _ptr(vis), int(eig_mode), int(k_rule), float(delta),
+                                       int(bool(shrink)), _ptr(evals), _ptr(evecs), _ptr(counts),
+                                       _ptr(proj), _stream(stream)))
+
+    def beamform(self, samples, scales, window, n_slots, beams, stream=None):
+        _check(lib().sf_beamform(self._h, _ptr(samples), _ptr(scales), int(window), int(n_slots),
+                                 _ptr(beams), _stream(stream)))
+
+    def accumulate_visibilities(self, vis, accum, stream=None):
+        _check(lib().sf_accumulate_visibilities(self._h, _ptr(vis), _ptr(accum), _stream(stream)))
+
+    def visibilities_to_float(self, accum, out, stream=None):
+        _check(lib().sf_visibilities_to_float(self._h, _ptr(accum), _ptr(out), _stream(stream)))
+
+    # ---- whole chains ----
+    def run_corr_beam(self, samples, scales, vis, beams, stream=None):
+        _check(lib().sf_run_corr_beam(self._h, _ptr(samples), _ptr(scales), _ptr(vis), _ptr(beams),
+                                      _stream(stream)))
+
+    def run_lambda_gpu(self, samples, scales, vis, evals, evecs, beams, stream=None):
+        _check(lib().sf_run_lambda_gpu(self._h, _ptr(samples), _ptr(scales), _ptr(vis), _ptr(evals),
+                                       _ptr(evecs), _ptr(beams), _stream(stream)))
+
+    def run_adaptive(self, samples, scales, k_rule, delta, shrink, vis, evals, evecs, counts, beams,
+                     stream=None):
+        _check(lib().sf_run_adaptive(self._h, _ptr(samples), _ptr(scales), int(k_rule), float(delta),
+                                     int(bool(shrink)), _ptr(vis), _ptr(evals), _ptr(evecs),
+                                     _ptr(counts), _ptr(beams), _stream(stream)))
+
+
+from .pipelines import (  # noqa: E402
+    GPUPipeline, LambdaAdaptiveBeamformedSpectraPipeline, LambdaCorrBeamOnlyGPUPipeline,
+    LambdaGPUPipeline, PacketData, SingleHostMemoryOutput)
+
+__all__ = ["Plan", "SfError", "lib", "header_symbols", "GPUPipeline", "LambdaGPUPipeline",
+           "LambdaCorrBeamOnlyGPUPipeline", "LambdaAdaptiveBeamformedSpectraPipeline",
+           "PacketData", "SingleHostMemoryOutput"]

@@ -1,0 +1,188 @@
+/*
+ * sf_capi.h - C ABI of the GB300 (sm_103a) spatial-filtering hot path.
+ *
+ * One integration of int8 complex voltages, in the reference's packet layout,
+ * goes through: correlation into int32 visibilities -> per-channel Hermitian
+ * covariance -> eigendecomposition -> RFI-subspace projection (I - U U^H) ->
+ * beamforming with projected weights (gains and fine-delay phasors folded in).
+ *
+ * Conventions (all arrays C-contiguous, little-endian):
+ *   samples  int8   [C][P+2][F][Tp][Rpp][Pol=2][2]      (LambdaConfig::InputPacketSamplesType)
+ *   scales   int16  [C][P+2][R][Pol]                    (LambdaConfig::PacketScalesType)
+ *   weights  fp16   [C][Pol][B][R][2]                   (BeamWeightsT<T>)
+ *   gains    float  [C][Pol][R][2]                      (LambdaConfig::AntennaGains)
+ *   vis      int32  [C][R(R+1)/2][Pol][Pol][2]          baseline(i,j)=j(j+1)/2+i, i<=j,
+ *                                                        value sum_t x_{i,p} conj(x_{j,q})
+ *   evals    float  [batch][R] ascending;  evecs float2 [batch][R(k)][R(l)] (component l of
+ *                                                        eigenvector k)
+ *   beams    fp16   [C][Pol][NB][T][2]                  (LambdaConfig::BeamOutputType)
+ * where R = F * Rpp receivers, T = P * Tp samples per integration.
+ *
+ * Every entry point is asynchronous on the given stream, never synchronises
+ * (except sf_plan_status, which says so), and returns an sf_status code.
+ * The CUDA stream argument is a cudaStream_t passed as void*.
+ */
+#ifndef SF_CAPI_H
+#define SF_CAPI_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum sf_status {
+  SF_OK = 0,
+  SF_ERR_INVALID_ARGUMENT = 1, /* bad shape, null pointer, out-of-range value */
+  SF_ERR_UNSUPPORTED = 2,      /* shape outside what the kernels implement */
+  SF_ERR_CUDA = 3,             /* a CUDA runtime call failed (sf_last_error has it) */
+  SF_ERR_DEVICE = 4,           /* a kernel reported an error bit (sf_plan_status) */
+  SF_ERR_NO_DEVICE = 5         /* no usable sm_103a device */
+} sf_status;
+
+/* Integration window inside the (P+2)-packet buffer. */
+typedef enum sf_window {
+  /* packets 0..P-1, no delay: LambdaCorrBeamOnlyGPUPipeline
+     (reference include/spatial/spatial.cuh:215-304) */
+  SF_WINDOW_PACKET = 0,
+  /* starts one packet in, shifted per FPGA by the sub-packet delay:
+     LambdaGPUPipeline / adaptive (reference include/spatial/spatial.cuh:1420-1506) */
+  SF_WINDOW_ALIGNED = 1
+} sf_window;
+
+/* Which covariance blocks are eigendecomposed. */
+typedef enum sf_eig_mode {
+  /* all Pol x Pol blocks, no whitening: batch C*Pol*Pol
+     (reference include/spatial/pipeline/lambda_gpu_pipeline.hpp:438-439, 494-501) */
+  SF_EIG_ALL_BLOCKS = 0,
+  /* same-polarisation blocks with diagonal whitening: batch C*Pol
+     (reference lambda_adaptive_beamformed_spectra_pipeline.hpp:648-686) */
+  SF_EIG_SAME_POL_WHITENED = 1
+} sf_eig_mode;
+
+/* How the number K of nulled modes is chosen per (channel, pol). */
+typedef enum sf_k_rule {
+  SF_K_FIXED = 0,       /* per-channel counts from sf_set_fixed_counts (default 0) */
+  SF_K_DETECT = 1,      /* K = #{lambda > p50 + delta (p80-p20)/1.6832}
+                           (reference include/spatial/spatial.cuh:900-950) */
+  SF_K_NOISE_FLOOR = 2  /* K = #{lambda > delta x median(lambda)} */
+} sf_k_rule;
+
+typedef struct sf_shape {
+  int32_t n_channels;             /* C */
+  int32_t n_fpgas;                /* F */
+  int32_t n_time_per_packet;      /* Tp */
+  int32_t n_receivers;            /* R = F * Rpp */
+  int32_t n_polarizations;        /* must be 2 */
+  int32_t n_receivers_per_packet; /* Rpp */
+  int32_t n_packets;              /* P packets per integration */
+  int32_t n_beams;                /* B */
+} sf_shape;
+
+typedef struct sf_plan sf_plan;
+
+/* Plan lifetime.  Replaces the constructors of LambdaGPUPipeline /
+ * LambdaCorrBeamOnlyGPUPipeline / LambdaAdaptiveBeamformedSpectraPipeline
+ * (reference include/spatial/pipeline/lambda_gpu_pipeline.hpp:784-797,
+ * lambda_corr_beam_only_gpu_pipeline.hpp:385-403,
+ * lambda_adaptive_beamformed_spectra_pipeline.hpp:1014-1036): allocates the
+ * plan's device state on the current device. */
+int sf_plan_create(const sf_shape *shape, sf_plan **out_plan);
+int sf_plan_destroy(sf_plan *plan);
+int sf_plan_get_shape(const sf_plan *plan, sf_shape *out_shape);
+
+/* Text of the last error on the calling thread (never NULL). */
+const char *sf_last_error(void);
+
+/* Reads and clears the plan's device error bits; synchronises `stream`.
+ * Replaces the reference's unread cuSOLVER info / CUDA_CHECK exits
+ * (reference include/spatial/logging.hpp:11-50). */
+int sf_plan_status(sf_plan *plan, void *stream, uint32_t *out_bits);
+
+/* ---- configuration (host arrays copied into plan device memory) ---------- */
+
+/* GPUPipeline::set_subpacket_delays (reference include/spatial/pipeline_base.hpp:15-17):
+ * one delay per FPGA in samples, each in [-Tp, Tp]; NULL resets to zero. */
+int sf_set_subpacket_delays(sf_plan *plan, const int32_t *h_delays, void *stream);
+
+/* GPUPipeline::set_antenna_gains (pipeline_base.hpp:18-20): complex gains
+ * [C][Pol][R][2] floats; NULL resets to 1. */
+int sf_set_antenna_gains(sf_plan *plan, const float *h_gains, void *stream);
+
+/* GPUPipeline::set_fine_delays (pipeline_base.hpp:21-22): per-receiver delays
+ * in ns folded into the weights as exp(-2 pi i f_c tau), f_c = base + (min_ch + c) bw. */
+int sf_set_fine_delays(sf_plan *plan, const float *h_delays_ns, double base_freq_hz,
+                       double channel_bw_hz, int32_t min_freq_ch, void *stream);
+
+/* Beam weights, BeamWeightsT<T> payload (reference include/spatial/pipeline/common.hpp:52-55). */
+int sf_set_weights(sf_plan *plan, const uint16_t *h_weights_f16, void *stream);
+
+/* Fixed K per channel (the -e map of the adaptive pipeline,
+ * lambda_adaptive_beamformed_spectra_pipeline.hpp:1160-1167); NULL resets to 0. */
+int sf_set_fixed_counts(sf_plan *plan, const int32_t *h_counts, void *stream);
+
+/* ---- stage kernels --------------------------------------------------------- */
+
+/* Correlate one integration into exact int32 visibilities on the tensor cores.
+ * Replaces packet_to_corr_input / aligned_to_corr_input + tcc::Correlator +
+ * corr_to_trimmed (reference spatial.cuh:55-304, lambda_gpu_pipeline.hpp:640-671,
+ * src/spatial.cu:176-200). */
+int sf_correlate(sf_plan *plan, const int8_t *d_samples, const int16_t *d_scales,
+                 int32_t window, int32_t *d_vis, void *stream);
+
+/* Covariance + eigendecomposition + K + projection + effective weights for
+ * each (channel, pol[, pol]) matrix.  Replaces unpack_triangular_baseline_batch,
+ * diagonalWhiten, cusolverDnXsyevBatched, detectSignalEigenmodeCounts,
+ * unwhitenEigenvectors, buildIdentityMinusProjection / shrink, and the ccglib
+ * weight projection (reference spatial.cuh:672-713, 900-1148;
+ * lambda_adaptive_beamformed_spectra_pipeline.hpp:648-794).
+ *   d_evals  [batch][R], d_evecs float2 [batch][R][R] (either may be NULL)
+ *   d_counts int32 [C][Pol] (SAME_POL mode only; may be NULL)
+ *   d_proj_f16 fp16 pairs [C][Pol][R][R] column-major projector (may be NULL)
+ * In SAME_POL mode the effective weights for sf_beamform (2B beams: original,
+ * projected) are left in plan memory. */
+int sf_covariance_eig(sf_plan *plan, const int32_t *d_vis, int32_t eig_mode, int32_t k_rule,
+                      float delta, int32_t shrink, float *d_evals, float *d_evecs,
+                      int32_t *d_counts, uint16_t *d_proj_f16, void *stream);
+
+/* Beamform with the plan's effective weights: n_slots = 1 uses W diag(d),
+ * n_slots = 2 uses the (original, projected) pair from sf_covariance_eig.
+ * Replaces aligned_to_col_maj_cons + weights permutation + ccglib GEMM +
+ * beam_ccglib_to_half_output (reference spatial.cuh:145-213, 376-418;
+ * lambda_gpu_pipeline.hpp:708-743). */
+int sf_beamform(sf_plan *plan, const int8_t *d_samples, const int16_t *d_scales, int32_t window,
+                int32_t n_slots, uint16_t *d_beams_f16, void *stream);
+
+/* Visibility integration across runs: accumulate int32 into int64
+ * (reference src/spatial.cu:62-71, 126-170) and convert the accumulator to the
+ * reference's float output with the gain/phasor factors applied
+ * (VisibilitiesOutputType, packet_formats.hpp:351-353; dump_visibilities,
+ * lambda_gpu_pipeline.hpp:1153-1194). */
+int sf_accumulate_visibilities(sf_plan *plan, const int32_t *d_vis, int64_t *d_accum,
+                               void *stream);
+int sf_visibilities_to_float(sf_plan *plan, const int64_t *d_accum, float *d_vis_f32,
+                             void *stream);
+
+/* ---- whole chains (what the drop-in pipelines run per buffer) -------------- */
+
+/* LambdaCorrBeamOnlyGPUPipeline::enqueue_main (lambda_corr_beam_only_gpu_pipeline.hpp:305-344). */
+int sf_run_corr_beam(sf_plan *plan, const int8_t *d_samples, const int16_t *d_scales,
+                     int32_t *d_vis, uint16_t *d_beams_f16, void *stream);
+
+/* LambdaGPUPipeline::execute_pipeline compute (lambda_gpu_pipeline.hpp:445-531):
+ * aligned window, all-blocks eigendecomposition, unprojected beams. */
+int sf_run_lambda_gpu(sf_plan *plan, const int8_t *d_samples, const int16_t *d_scales,
+                      int32_t *d_vis, float *d_evals, float *d_evecs, uint16_t *d_beams_f16,
+                      void *stream);
+
+/* Adaptive null/shrink chain (lambda_adaptive_beamformed_spectra_pipeline.hpp:563-798):
+ * corr -> whitened eig -> K -> I - U U^H (or shrink) -> W P -> 2B beams. */
+int sf_run_adaptive(sf_plan *plan, const int8_t *d_samples, const int16_t *d_scales,
+                    int32_t k_rule, float delta, int32_t shrink, int32_t *d_vis, float *d_evals,
+                    float *d_evecs, int32_t *d_counts, uint16_t *d_beams_f16, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SF_CAPI_H */

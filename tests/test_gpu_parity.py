@@ -1,0 +1,271 @@
+"""CUDA path vs the oracle and the reference's golden values (GPU only).
+
+Integer work (visibilities) must be bit-exact.  Floating-point tolerances:
+  beams       fp16 output of an fp32 sum: |y - y_ref| <= 2^-9 |y_ref| + 2^-6 (abs)
+  eigenvalues |lambda - lambda_lapack| <= 2e-5 ||A||_2  (fp32 Jacobi vs FP64 LAPACK)
+  residual    ||A v - lambda v|| <= 1e-4 ||A||_2, orthogonality ||V^H V - I|| <= 1e-4
+  projector   ||P - P_ref||_max <= 2e-3 when the nulled eigenvalues are separated
+"""
+import numpy as np
+import pytest
+import torch
+
+import sf_oracle as orc
+import sfgb
+from case_checks import check_case, oracle_outputs, oracle_shape, _power
+from reference_cases import build_cases
+
+pytestmark = pytest.mark.gpu
+
+CASES = build_cases()
+
+
+def _dev(x, dtype):
+    return torch.as_tensor(np.ascontiguousarray(x)).to(device="cuda").view(dtype)
+
+
+def gpu_case_outputs(case):
+    C, F, Tp, R, Rpp, P, B = case.shape
+    out = sfgb.SingleHostMemoryOutput()
+    if case.path == "corr_beam":
+        pipe = sfgb.LambdaCorrBeamOnlyGPUPipeline(case.shape, case.weights)
+    elif case.path == "lambda_gpu":
+        pipe = sfgb.LambdaGPUPipeline(case.shape, case.weights)
+    else:
+        a = case.adaptive
+        pipe = sfgb.LambdaAdaptiveBeamformedSpectraPipeline(
+            case.shape, case.weights, nr_signal_eigenvectors={0: a.get("k", 0)},
+            shrink_eigenvalues=a.get("shrink", False), detect_signal_eigenmodes=a.get("detect", False),
+            detection_threshold_delta=a.get("delta", 3.0))
+    pipe.set_output(out)
+    if case.delays is not None:
+        pipe.set_subpacket_delays(case.delays)
+    if case.gains is not None:
+        pipe.set_antenna_gains(case.gains)
+    pipe.execute_pipeline(sfgb.PacketData(case.samples, case.scales))
+    pipe.dump_visibilities()
+    rc, bits = pipe.plan.status()
+    assert rc == 0 and bits == 0, f"device status bits 0x{bits:x}"
+    res = {"beam_half": out.beam_data.astype(np.float32), "vis": out.visibilities}
+    if out.eigenvalues is not None:
+        res["evals"] = out.eigenvalues
+        ev = out.eigenvectors
+        res["evecs"] = ev[..., 0] + 1j * ev[..., 1]
+    if out.nulled_eigenmode_counts is not None:
+        res["counts"] = out.nulled_eigenmode_counts
+    pipe.plan.close()
+    return res
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c.name for c in CASES])
+def test_reference_goldens_through_the_c_abi(case):
+    out = gpu_case_outputs(case)
+    check_case(case, out)
+    ref = oracle_outputs(case)
+    assert np.array_equal(out["vis"], ref["vis"]), f"{case.name}: float visibilities differ from oracle"
+
+
+def test_shrink_rank_two_exceeds_null_on_gpu():
+    case = next(c for c in CASES if c.name == "AdaptiveShrinkRankTwo")
+    import copy
+    null_case = copy.copy(case)
+    null_case.adaptive = {"k": 1, "shrink": False}
+    pn = _power(gpu_case_outputs(null_case)["beam_half"])
+    ps = _power(gpu_case_outputs(case)["beam_half"])
+    assert ps > pn + 1e-6
+
+
+# --------------------------------------------------------------------------
+# Correlator: bit-exact int32 against the exact-integer oracle
+# --------------------------------------------------------------------------
+def _correlate_gpu(sh, samples, scales, window, delays=None):
+    plan = sfgb.Plan(sh.C, sh.F, sh.Tp, sh.R, sh.Rpp, sh.P, sh.B)
+    if delays is not None:
+        plan.set_subpacket_delays(delays)
+    s = _dev(samples, torch.int8)
+    sc = _dev(scales, torch.int16)
+    vis = torch.full(plan.vis_shape(), -7, dtype=torch.int32, device="cuda")
+    plan.correlate(s, sc, window, vis)
+    torch.cuda.synchronize()
+    rc, bits = plan.status()
+    assert rc == 0 and bits == 0, f"device status 0x{bits:x}"
+    plan.close()
+    return vis.cpu().numpy()
+
+
+@pytest.mark.parametrize("R,F,Tp,P,window,delays", [
+    (36, 4, 64, 4, sfgb.SF_WINDOW_ALIGNED, [0, 5, -7, 64]),
+    (36, 4, 64, 4, sfgb.SF_WINDOW_PACKET, None),
+    (4, 1, 8, 1, sfgb.SF_WINDOW_ALIGNED, [0]),
+    (6, 3, 8, 3, sfgb.SF_WINDOW_ALIGNED, [0, 3, -4]),
+    (16, 2, 64, 2, sfgb.SF_WINDOW_ALIGNED, [-64, 17]),
+    (32, 4, 32, 5, sfgb.SF_WINDOW_ALIGNED, [1, 2, 3, -32]),
+    (40, 4, 64, 3, sfgb.SF_WINDOW_ALIGNED, [0, 0, 1, 1]),
+    (48, 6, 16, 9, sfgb.SF_WINDOW_ALIGNED, [0, -16, 16, 5, -5, 9]),
+])
+def test_correlator_bit_exact_random(R, F, Tp, P, window, delays):
+    sh = orc.Shape(3, F, Tp, R, R // F, P, 1)
+    rng = np.random.default_rng(R * 1000 + Tp)
+    samples = rng.integers(-128, 128, size=sh.samples_shape(), dtype=np.int8)
+    scales = rng.integers(-1, 2, size=sh.scales_shape()).astype(np.int16)
+    off = orc.sample_offsets(sh, delays, mode="aligned" if window == sfgb.SF_WINDOW_ALIGNED else "packet")
+    re, im = orc.aligned_samples(sh, samples, scales, off)
+    ref = orc.correlate(sh, re, im)
+    got = _correlate_gpu(sh, samples, scales, window, delays)
+    assert np.array_equal(got, ref)
+
+
+def test_correlator_exact_at_full_scale():
+    """Every sample at -128/127 over 4096 samples: partial sums reach 2^27, so
+    exactness relies on the 512-sample fp32 chunks drained into int32."""
+    sh = orc.Shape(2, 4, 64, 36, 9, 64, 1)
+    rng = np.random.default_rng(7)
+    samples = np.where(rng.random(sh.samples_shape()) < 0.5, -128, 127).astype(np.int8)
+    scales = np.ones(sh.scales_shape(), np.int16)
+    re, im = orc.aligned_samples(sh, samples, scales, orc.sample_offsets(sh))
+    ref = orc.correlate(sh, re, im)
+    assert np.abs(ref).max() > 2 ** 24
+    got = _correlate_gpu(sh, samples, scales, sfgb.SF_WINDOW_ALIGNED, [0, 0, 0, 0])
+    assert np.array_equal(got, ref)
+
+
+def test_correlator_many_channels_persistent_loop():
+    """More channels than SMs: every CTA walks several channels."""
+    sh = orc.Shape(400, 1, 16, 8, 8, 2, 1)
+    rng = np.random.default_rng(11)
+    samples = rng.integers(-128, 128, size=sh.samples_shape(), dtype=np.int8)
+    scales = rng.integers(0, 3, size=sh.scales_shape()).astype(np.int16)
+    re, im = orc.aligned_samples(sh, samples, scales, orc.sample_offsets(sh, [3]))
+    ref = orc.correlate(sh, re, im)
+    got = _correlate_gpu(sh, samples, scales, sfgb.SF_WINDOW_ALIGNED, [3])
+    assert np.array_equal(got, ref)
+
+
+# --------------------------------------------------------------------------
+# Eigensolver, projector, beams on LAMBDA-shaped synthetic data
+# --------------------------------------------------------------------------
+def _run_adaptive_gpu(sh, samples, scales, weights, k_rule, delta, shrink=False, fixed=None,
+                      gains=None, fine=None):
+    plan = sfgb.Plan(sh.C, sh.F, sh.Tp, sh.R, sh.Rpp, sh.P, sh.B)
+    plan.set_weights(weights)
+    if fixed is not None:
+        plan.set_fixed_counts(fixed)
+    if gains is not None:
+        plan.set_antenna_gains(gains)
+    if fine is not None:
+        plan.set_fine_delays(*fine)
+    s = _dev(samples, torch.int8)
+    sc = _dev(scales, torch.int16)
+    vis = torch.empty(plan.vis_shape(), dtype=torch.int32, device="cuda")
+    ev = torch.empty((sh.C, 2, sh.R), dtype=torch.float32, device="cuda")
+    vec = torch.empty((sh.C, 2, sh.R, sh.R, 2), dtype=torch.float32, device="cuda")
+    cnt = torch.empty((sh.C, 2), dtype=torch.int32, device="cuda")
+    beams = torch.empty(plan.beams_shape(2), dtype=torch.float16, device="cuda")
+    plan.run_adaptive(s, sc, k_rule, delta, shrink, vis, ev, vec, cnt, beams)
+    torch.cuda.synchronize()
+    rc, bits = plan.status()
+    assert rc == 0 and bits == 0, f"device status 0x{bits:x}"
+    out = {"vis": vis.cpu().numpy(), "evals": ev.cpu().numpy(), "counts": cnt.cpu().numpy(),
+           "beams": beams.cpu().numpy().astype(np.float32)}
+    v = vec.cpu().numpy()
+    out["evecs"] = v[..., 0] + 1j * v[..., 1]
+    plan.close()
+    return out
+
+
+@pytest.fixture(scope="module")
+def lambda_cfg():
+    sh = orc.Shape(16, 4, 64, 36, 9, 16, 4)
+    samples, scales, rfi = orc.synth_inputs(sh, seed=0, n_interferers=2, frac_channels=0.5)
+    weights = orc.synth_weights(sh)
+    return sh, samples, scales, weights, rfi
+
+
+def test_eig_against_lapack(lambda_cfg):
+    sh, samples, scales, weights, rfi = lambda_cfg
+    got = _run_adaptive_gpu(sh, samples, scales, weights, sfgb.SF_K_FIXED, 0.0, fixed=np.full(sh.C, 2))
+    ref = orc.adaptive_chain(sh, samples, scales, weights, k_fixed=np.full(sh.C, 2))
+    assert np.array_equal(got["vis"], ref["vis"])
+    vc = orc.scaled_visibilities(sh, ref["vis"], orc.receiver_factors(sh))
+    for p in range(2):
+        m = orc.unpack_hermitian(sh, vc, p, p)
+        for c in range(sh.C):
+            a, _ = orc.whiten(m[c])
+            norm = np.linalg.norm(a, 2)
+            lam = got["evals"][c, p].astype(np.float64)
+            assert np.all(np.diff(lam) >= -1e-6 * norm)
+            assert np.max(np.abs(lam - ref["evals"][c, p])) <= 2e-5 * norm
+    # eigenvector quality on the whitened matrices: residual and orthogonality
+    sh1 = sh
+    plan = sfgb.Plan(sh1.C, sh1.F, sh1.Tp, sh1.R, sh1.Rpp, sh1.P, sh1.B)
+    vis = _dev(ref["vis"].astype(np.int32), torch.int32)
+    ev = torch.empty((sh.C, 2, sh.R), dtype=torch.float32, device="cuda")
+    vec = torch.empty((sh.C, 2, sh.R, sh.R, 2), dtype=torch.float32, device="cuda")
+    plan.covariance_eig(vis, sfgb.SF_EIG_SAME_POL_WHITENED, sfgb.SF_K_FIXED, 0.0, True, ev, vec)
+    torch.cuda.synchronize()
+    lam = ev.cpu().numpy().astype(np.float64)
+    v = vec.cpu().numpy()
+    V = (v[..., 0] + 1j * v[..., 1]).astype(np.complex128)
+    plan.close()
+    for p in range(2):
+        m = orc.unpack_hermitian(sh, vc, p, p)
+        for c in range(sh.C):
+            a, _ = orc.whiten(m[c])
+            norm = np.linalg.norm(a, 2)
+            U = V[c, p].T  # columns = eigenvectors
+            res = np.linalg.norm(a @ U - U * lam[c, p][None, :], axis=0).max()
+            assert res <= 1e-4 * norm
+            assert np.abs(U.conj().T @ U - np.eye(sh.R)).max() <= 1e-4
+
+
+def test_adaptive_null_projection_and_beams(lambda_cfg):
+    sh, samples, scales, weights, rfi = lambda_cfg
+    fixed = np.full(sh.C, 2)
+    got = _run_adaptive_gpu(sh, samples, scales, weights, sfgb.SF_K_FIXED, 0.0, fixed=fixed)
+    ref = orc.adaptive_chain(sh, samples, scales, weights, k_fixed=fixed)
+    yr = ref["beams"]
+    yb = got["beams"][..., 0] + 1j * got["beams"][..., 1]
+    err = np.abs(yb - yr)
+    tol = 2.0 ** -9 * np.abs(yr) + 2.0 ** -6 + 1e-3 * np.abs(yr).max(axis=-1, keepdims=True)
+    assert np.all(err[:, :, :sh.B] <= 2.0 ** -9 * np.abs(yr[:, :, :sh.B]) + 2.0 ** -6)
+    assert np.all(err <= tol)
+    # projected eigenvectors (the RFI subspace) match LAPACK's: compare the projectors
+    for c in range(sh.C):
+        for p in range(2):
+            if not rfi[c]:
+                continue
+            U = got["evecs"][c, p].T[:, -2:]
+            Ur = ref["evecs"][c, p].T[:, -2:]
+            assert np.abs(U @ U.conj().T - Ur @ Ur.conj().T).max() <= 2e-3
+
+
+def test_adaptive_detection_counts_match_oracle(lambda_cfg):
+    sh, samples, scales, weights, rfi = lambda_cfg
+    got = _run_adaptive_gpu(sh, samples, scales, weights, sfgb.SF_K_DETECT, 3.0)
+    ref = orc.adaptive_chain(sh, samples, scales, weights, detect=True, delta=3.0)
+    # detection on the device runs on fp32 eigenvalues; decide with the oracle
+    # rule applied to the device's own eigenvalues and compare
+    for c in range(sh.C):
+        for p in range(2):
+            assert got["counts"][c, p] == orc.detect_k_f32(got["evals"][c, p], 3.0)
+    assert np.mean(got["counts"] == ref["counts"]) >= 0.9
+    # interfered channels detect both interferers
+    assert np.all(got["counts"][rfi] >= 2)
+
+
+def test_gains_and_fine_delays_folded(lambda_cfg):
+    sh, samples, scales, weights, rfi = lambda_cfg
+    rng = np.random.default_rng(5)
+    gains = (rng.normal(1, 0.1, (sh.C, 2, sh.R)) + 1j * rng.normal(0, 0.1, (sh.C, 2, sh.R))).astype(np.complex64)
+    tau = rng.uniform(-5, 5, sh.R).astype(np.float32)
+    fine = (tau, 0.0, 781250.0, 64)
+    fixed = np.full(sh.C, 1)
+    got = _run_adaptive_gpu(sh, samples, scales, weights, sfgb.SF_K_FIXED, 0.0, fixed=fixed,
+                            gains=gains, fine=fine)
+    ph = orc.fine_delay_phasors(sh, tau, 0.0, 781250.0, 64)
+    d = orc.receiver_factors(sh, gains=gains, phasors=ph)
+    ref = orc.adaptive_chain(sh, samples, scales, weights, k_fixed=fixed, d=d)
+    yr = ref["beams"]
+    yb = got["beams"][..., 0] + 1j * got["beams"][..., 1]
+    tol = 2.0 ** -9 * np.abs(yr) + 2.0 ** -6 + 2e-3 * np.abs(yr).max(axis=-1, keepdims=True)
+    assert np.all(np.abs(yb - yr) <= tol)
