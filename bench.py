@@ -1,0 +1,479 @@
+#!/usr/bin/env python3
+"""Benchmark of the spatial-filtering hot path on GB300.
+
+Workload (one step = one integration of every channel through the chain):
+LAMBDA-scale plain path -- 36 antennas (4 FPGAs x 9), 2 polarisations, 384
+channels, 4096 int8 complex samples per integration (64 packets x 64), noise
+sigma 16 plus 2 narrowband interferers in a random 10% of channels at INR
+20 dB; correlate -> per-channel per-pol 36x36 whitened eigendecomposition ->
+project out k = 2 -> 8 beams (original + projected weight slots) with
+fine-delay phasors exp(-2 pi i f_c tau), tau ~ U(-5, 5) ns, f_c from the
+781.25 kHz channel plan.  Seeded synthetic data stands in for telescope data.
+
+Metric: channel-integrations/s (channels x integrations per second).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the same chain (oracle/
+sf_oracle.c, OpenMP over all host threads); the reference's own GPU build
+(TCC + ccglib + cuSOLVER) cannot be built here (its submodules are absent).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "cuda-spatial-filtering_gb300"))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+METRIC = "chan-integrations/s corr->eig-null->beam"
+UNIT = "chan-integrations/s"
+
+# LAMBDA-scale configuration
+C, F, TP, RPP, P, B = 384, 4, 64, 9, 64, 8
+R = F * RPP
+T = P * TP
+K_NULL = 2
+MIN_FREQ_CH = 64
+CHANNEL_BW = 781250.0
+
+WORKLOAD = {
+    "workload": "lambda_scale_adaptive_null",
+    "channels": C, "antennas": R, "polarizations": 2, "samples_per_integration": T,
+    "fpgas": F, "receivers_per_packet": RPP, "samples_per_packet": TP,
+    "beams": B, "beam_slots": 2, "k_null": K_NULL, "interferers": 2,
+    "interferer_channel_fraction": 0.1, "inr_db": 20.0, "fine_delay_ns": 5.0,
+    "l2": "inputs (233.6 MB samples) larger than L2 (129 MB); no flush",
+}
+
+# Algorithmic bytes per channel-integration (each object touched once):
+# int8 input 2 R Pol T + int32 visibilities 8 R(R+1)/2 Pol^2 + beams
+BYTES_IN = 2 * R * 2 * T
+BYTES_VIS = 8 * (R * (R + 1) // 2) * 4
+BYTES_BEAMS_FP16 = 2 * B * 2 * T * 4  # 2B fp16 complex beams
+BYTES_PER_UNIT = BYTES_IN + BYTES_VIS + 8 * B * 2 * T  # fp32-complex beam convention
+KERNEL_BYTES = {
+    "sf_corr_kernel": BYTES_IN + BYTES_VIS,
+    "sf_beam_kernel": BYTES_IN + BYTES_BEAMS_FP16,
+}
+
+
+def _set_channels(n):
+    global C
+    C = int(n)
+    WORKLOAD["channels"] = C
+
+
+def run_stage_only(args):
+    """Warm-up + a few launches of one stage kernel on resident inputs (the
+    command an ncu capture wraps); prints the mean launch time."""
+    import torch
+    import sfgb
+    sh, samples, scales, weights, tau, rfi = make_inputs(seed=0)
+    plan = sfgb.Plan(C, F, TP, R, RPP, P, B)
+    plan.set_weights(weights)
+    plan.set_fixed_counts(np.full(C, K_NULL, np.int32))
+    stream = torch.cuda.Stream()
+    d_s = [torch.as_tensor(samples).cuda(), torch.as_tensor(np.roll(samples, 1, axis=0)).cuda()]
+    d_sc = [torch.as_tensor(scales).cuda()] * 2
+    vis = torch.empty(plan.vis_shape(), dtype=torch.int32, device="cuda")
+    ev = torch.empty((C, 2, R), dtype=torch.float32, device="cuda")
+    cnt = torch.empty((C, 2), dtype=torch.int32, device="cuda")
+    beams = torch.empty(plan.beams_shape(2), dtype=torch.float16, device="cuda")
+    plan.correlate(d_s[0], d_sc[0], sfgb.SF_WINDOW_ALIGNED, vis, stream=stream)
+    name = {"corr": "sf_corr_kernel", "eig": "sf_eig_kernel", "beam": "sf_beam_kernel"}[args.only_stage]
+    res = _stage_breakdown(plan, d_s, d_sc, vis, ev, cnt, beams, stream, args.steps, only=name)
+    rc, bits = plan.status(stream)
+    if rc != 0:
+        raise RuntimeError(f"device status 0x{bits:x}")
+    print(json.dumps({"stage": name, "channels": C, "ms": res[name]["ms"]}))
+    return 0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def make_inputs(seed=0):
+    import sf_oracle as orc
+    sh = orc.Shape(C, F, TP, R, RPP, P, B)
+    samples, scales, rfi = orc.synth_inputs(sh, seed=seed, n_interferers=2, inr_db=20.0, frac_channels=0.1)
+    weights = orc.synth_weights(sh, seed=1)
+    rng = np.random.default_rng(2)
+    tau = rng.uniform(-5.0, 5.0, R).astype(np.float32)
+    return sh, samples, scales, weights, tau, rfi
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(_local_rank()), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                rows.append((float(parts[0]), float(parts[1]), parts[3:7]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, flags in rows for i, f in enumerate(flags) if f.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def _local_rank():
+    return int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def run_ours(args, world, rank):
+    import torch
+    import sfgb
+    import sf_oracle as orc
+
+    torch.cuda.set_device(_local_rank())
+    dev = torch.device("cuda", _local_rank())
+    sh, samples, scales, weights, tau, rfi = make_inputs(seed=rank)
+    plan = sfgb.Plan(C, F, TP, R, RPP, P, B)
+    plan.set_weights(weights)
+    plan.set_fixed_counts(np.full(C, K_NULL, np.int32))
+    plan.set_fine_delays(tau, 0.0, CHANNEL_BW, MIN_FREQ_CH)
+    stream = torch.cuda.Stream(device=dev)
+    # two resident input sets, alternated step to step
+    d_s = [torch.as_tensor(samples).to(dev), torch.as_tensor(np.roll(samples, 1, axis=0)).to(dev)]
+    d_sc = [torch.as_tensor(scales).to(dev), torch.as_tensor(scales).to(dev)]
+    vis = torch.empty(plan.vis_shape(), dtype=torch.int32, device=dev)
+    ev = torch.empty((C, 2, R), dtype=torch.float32, device=dev)
+    cnt = torch.empty((C, 2), dtype=torch.int32, device=dev)
+    beams = torch.empty(plan.beams_shape(2), dtype=torch.float16, device=dev)
+
+    def step(i):
+        plan.run_adaptive(d_s[i % 2], d_sc[i % 2], sfgb.SF_K_FIXED, 0.0, False, vis, ev, None, cnt, beams,
+                          stream=stream)
+
+    for i in range(args.warmup):
+        step(i)
+    stream.synchronize()
+    rc, bits = plan.status(stream)
+    if rc != 0:
+        raise RuntimeError(f"device status 0x{bits:x} after warm-up")
+    # correctness gate on this very workload: visibilities bit-exact vs the C oracle
+    _check_against_oracle(plan, d_s[0], d_sc[0], vis, samples, scales, stream)
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler()
+    clocks.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(args.steps):
+        step(i)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    ms_per_step = ms / args.steps
+    value = world * C / (ms_per_step / 1e3)
+
+    # per-kernel breakdown (stages launched one at a time on the same stream)
+    kernels = _stage_breakdown(plan, d_s, d_sc, vis, ev, cnt, beams, stream, max(3, args.steps))
+    e2e = _e2e(plan, samples, scales, stream, max(3, args.steps // 2), dev)
+    rc, bits = plan.status(stream)
+    if rc != 0:
+        raise RuntimeError(f"device status 0x{bits:x} after timing")
+
+    hbm, tf, peak_kind = measured_peaks()
+    dom = max(kernels, key=lambda k: kernels[k]["ms"])
+    dom_ms = kernels[dom]["ms"]
+    if dom in KERNEL_BYTES:
+        achieved = KERNEL_BYTES[dom] * C / (dom_ms / 1e3) / 1e9
+        roof = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4), "peak_source": peak_kind,
+                "bytes_per_launch": KERNEL_BYTES[dom] * C, "traffic": None}
+    else:
+        # the eigensolver: report its HBM traffic against the HBM peak, plus matrices/s
+        byts = (BYTES_VIS + 2 * 2 * B * R * 8) * C
+        achieved = byts / (dom_ms / 1e3) / 1e9
+        roof = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4), "peak_source": peak_kind, "bytes_per_launch": byts,
+                "traffic": None, "note": "latency-bound eigensolver; matrices/s = %.0f" % (2 * C / (dom_ms / 1e3))}
+    prof = ROOT / "profiles" / "traffic.json"
+    if prof.exists():
+        try:
+            tr = json.loads(prof.read_text()).get(dom)
+            if tr:
+                roof["traffic"] = tr
+        except Exception:
+            pass
+
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int8 in; fp16 tensor products, exact int32 visibilities; fp32 eig/beam",
+        "data": "synthetic (seeded LAMBDA-shaped int8 voltages with interferers)",
+        "config": dict(WORKLOAD, parallelism=f"channel shards x{world}" if world > 1 else "single GPU"),
+        "roofline": roof,
+        "kernels_ms": {k: round(v["ms"], 4) for k, v in kernels.items()},
+        "e2e": e2e,
+        "gpu_launches": 3 * args.steps,
+        "clocks": clk,
+    }
+    return line
+
+
+def _check_against_oracle(plan, d_s, d_sc, vis, samples, scales, stream):
+    import sf_oracle as orc
+    import sf_oracle_c as sfc
+    sh = orc.Shape(C, F, TP, R, RPP, P, B)
+    nchk = 8
+    plan.correlate(d_s, d_sc, 1, vis, stream=stream)
+    stream.synchronize()
+    got = vis[:nchk].cpu().numpy()
+    sub = orc.Shape(nchk, F, TP, R, RPP, P, B)
+    ref = sfc.correlate(sub, samples[:nchk], scales[:nchk], orc.sample_offsets(sub), nthreads=os.cpu_count())
+    if not np.array_equal(got, ref):
+        raise RuntimeError("bench workload: GPU visibilities differ from the oracle")
+
+
+def _stage_breakdown(plan, d_s, d_sc, vis, ev, cnt, beams, stream, reps, only=None):
+    import torch
+    import sfgb
+    stages = {
+        "sf_corr_kernel": lambda i: plan.correlate(d_s[i % 2], d_sc[i % 2], sfgb.SF_WINDOW_ALIGNED, vis, stream=stream),
+        "sf_eig_kernel": lambda i: plan.covariance_eig(vis, sfgb.SF_EIG_SAME_POL_WHITENED, sfgb.SF_K_FIXED, 0.0,
+                                                       False, ev, None, cnt, None, stream=stream),
+        "sf_beam_kernel": lambda i: plan.beamform(d_s[i % 2], d_sc[i % 2], sfgb.SF_WINDOW_ALIGNED, 2, beams,
+                                                  stream=stream),
+    }
+    out = {}
+    for name, fn in stages.items():
+        if only is not None and name != only:
+            continue
+        for i in range(2):
+            fn(i)
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(reps):
+            fn(i)
+        e1.record(stream)
+        e1.synchronize()
+        out[name] = {"ms": e0.elapsed_time(e1) / reps}
+    return out
+
+
+def _e2e(plan, samples, scales, stream, steps, dev):
+    """Same chain through the public API from pinned host buffers: every step
+    copies its inputs host->device and reads its beams, visibilities and
+    counts back; copies of neighbouring steps overlap compute on separate
+    streams (two device buffer sets)."""
+    import torch
+    import sfgb
+    h_s = torch.as_tensor(samples).pin_memory()
+    h_sc = torch.as_tensor(scales).pin_memory()
+    nb = 2
+    d_s = [torch.empty_like(h_s, device=dev) for _ in range(nb)]
+    d_sc = [torch.empty_like(h_sc, device=dev) for _ in range(nb)]
+    vis = [torch.empty(plan.vis_shape(), dtype=torch.int32, device=dev) for _ in range(nb)]
+    cnt = [torch.empty((C, 2), dtype=torch.int32, device=dev) for _ in range(nb)]
+    beams = [torch.empty(plan.beams_shape(2), dtype=torch.float16, device=dev) for _ in range(nb)]
+    h_beams = [torch.empty(plan.beams_shape(2), dtype=torch.float16).pin_memory() for _ in range(nb)]
+    h_vis = [torch.empty(plan.vis_shape(), dtype=torch.int32).pin_memory() for _ in range(nb)]
+    h_cnt = [torch.empty((C, 2), dtype=torch.int32).pin_memory() for _ in range(nb)]
+    s_in, s_out = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+    ev_in = [torch.cuda.Event() for _ in range(nb)]
+    ev_done = [torch.cuda.Event() for _ in range(nb)]
+    ev_out = [torch.cuda.Event() for _ in range(nb)]
+
+    def run(n):
+        for i in range(n):
+            b = i % nb
+            with torch.cuda.stream(s_in):
+                s_in.wait_event(ev_done[b])  # compute of step i-nb has consumed this buffer
+                d_s[b].copy_(h_s, non_blocking=True)
+                d_sc[b].copy_(h_sc, non_blocking=True)
+                ev_in[b].record(s_in)
+            stream.wait_event(ev_in[b])
+            stream.wait_event(ev_out[b])  # beams of step i-nb have been read back
+            plan.run_adaptive(d_s[b], d_sc[b], sfgb.SF_K_FIXED, 0.0, False, vis[b], None, None, cnt[b],
+                              beams[b], stream=stream)
+            ev_done[b].record(stream)
+            with torch.cuda.stream(s_out):
+                s_out.wait_event(ev_done[b])
+                h_beams[b].copy_(beams[b], non_blocking=True)
+                h_vis[b].copy_(vis[b], non_blocking=True)
+                h_cnt[b].copy_(cnt[b], non_blocking=True)
+                ev_out[b].record(s_out)
+
+    run(2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s_in)
+    run(steps)
+    for b in range(nb):
+        s_out.wait_event(ev_out[b])
+    e1.record(s_out)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    wall = (time.perf_counter() - t0) / steps * 1e3
+    bi = h_s.numel() * h_s.element_size() + h_sc.numel() * h_sc.element_size()
+    bo = sum(t.numel() * t.element_size() for t in (h_beams[0], h_vis[0], h_cnt[0]))
+    return {"value": round(C / (ms / 1e3), 1), "unit": UNIT, "h2d_bytes_per_step": int(bi),
+            "d2h_bytes_per_step": int(bo), "ms_per_step": round(ms, 4), "host_wall_ms_per_step": round(wall, 4),
+            "overlap": "double-buffered: H2D(i+1) || compute(i) || D2H(i-1)"}
+
+
+def cpu_baseline(sample_channels=None, nthreads=None, reps=1):
+    """CPU restatement of the same chain (oracle/sf_oracle.c) on a bounded
+    sample of the workload's channels."""
+    import sf_oracle as orc
+    import sf_oracle_c as sfc
+    sh, samples, scales, weights, tau, rfi = make_inputs(seed=0)
+    nthreads = nthreads or sfc.max_threads()
+    n = sample_channels or C
+    sub = orc.Shape(n, F, TP, R, RPP, P, B)
+    d = orc.receiver_factors(sub, phasors=orc.fine_delay_phasors(sub, tau, 0.0, CHANNEL_BW, MIN_FREQ_CH))
+    off = orc.sample_offsets(sub)
+    args = (sub, samples[:n], scales[:n], off, weights[:n].astype(np.float32), d)
+    kw = dict(fixed_k=np.full(n, K_NULL), k_rule=0, nthreads=nthreads, want=("counts", "beams"))
+    sfc.adaptive_chain(*args, **kw)  # warm-up (page-in, thread pool)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        sfc.adaptive_chain(*args, **kw)
+    dt = (time.perf_counter() - t0) / reps
+    return {"value": round(n / dt, 2), "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{n} of {C} channels of one integration (full chain: exact int64 correlation, "
+                      f"FP64 Jacobi, I-UU^H, W P, 16 beams), {reps} rep(s), OpenMP over channels",
+            "seconds_per_rep": round(dt, 3)}
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the CPU restatement on all host threads, per step a
+    bounded sample of the integration (channels), reported per channel."""
+    import sf_oracle_c as sfc
+    nthreads = sfc.max_threads()
+    n = args.ref_channels
+    for _ in range(args.warmup):
+        cpu_baseline(sample_channels=n, nthreads=nthreads, reps=1)
+    times = []
+    for _ in range(args.steps):
+        r = cpu_baseline(sample_channels=n, nthreads=nthreads, reps=1)
+        times.append(r["seconds_per_rep"])
+    dt = sum(times) / len(times)
+    value = n / dt
+    return {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int64 corr, f64 eig/beam",
+        "data": "synthetic (seeded LAMBDA-shaped int8 voltages with interferers)",
+        "config": dict(WORKLOAD, parallelism="host threads"), "impl": "reference",
+        "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": f"{n} of {C} channels per step (reference GPU build unavailable: "
+                                   "TCC/ccglib submodules absent; CPU restatement of the chain)"},
+        "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--ref-channels", type=int, default=384)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--channels", type=int, default=C,
+                    help="channels per integration (default: the 384-channel workload)")
+    ap.add_argument("--only-stage", choices=["corr", "eig", "beam"],
+                    help="launch one stage kernel only (for a profiler capture)")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    _set_channels(args.channels)
+    if args.only_stage:
+        return run_stage_only(args)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        print(json.dumps(run_reference(args, world, rank)), flush=True)
+        return 0
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    line = run_ours(args, world, rank)
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(sample_channels=None)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
