@@ -89,6 +89,9 @@ int upload_offsets(sf_plan *p, cudaStream_t s) {
 
 }  // namespace
 
+// Lets other translation units of the library report through sf_last_error.
+int sf_internal_set_error(int code, const char *msg) { return set_err(code, "%s", msg); }
+
 extern "C" {
 
 const char *sf_last_error(void) { return g_err; }

@@ -68,6 +68,8 @@ _SIGS = {
     "sf_run_corr_beam": ([_P, _P, _P, _P, _P, _P], ctypes.c_int),
     "sf_run_lambda_gpu": ([_P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "sf_run_adaptive": ([_P, _P, _P, _I32, ctypes.c_float, _I32, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "sf_run_adaptive_noalloc": ([ctypes.POINTER(ShapeStruct), _P, _P, _P, _P, _P, _P, _I32, ctypes.c_float,
+                                 _I32, _P, _P, _P, _P], ctypes.c_int),
 }
 
 
@@ -75,6 +77,18 @@ def header_symbols():
     """Function names declared in include/sf_capi.h."""
     text = HEADER.read_text()
     return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(sf_\w+)\s*\(", text, re.M)))
+
+
+def run_adaptive_noalloc(shape, samples, scales, weights, k_rule, delta, shrink, beams, factors=None,
+                         delays=None, fixed_counts=None, counts=None, status=None, stream=None):
+    """sf_run_adaptive_noalloc over caller-owned device tensors (no plan).
+    ``shape`` is (C, F, Tp, R, Rpp, P, B)."""
+    C, F, Tp, R, Rpp, P, B = shape
+    st = ShapeStruct(C, F, Tp, R, 2, Rpp, P, B)
+    _check(lib().sf_run_adaptive_noalloc(ctypes.byref(st), _ptr(samples), _ptr(scales), _ptr(weights),
+                                         _ptr(factors), _ptr(delays), _ptr(fixed_counts), int(k_rule),
+                                         float(delta), int(bool(shrink)), _ptr(counts), _ptr(beams),
+                                         _ptr(status), _stream(stream)))
 
 
 def lib():

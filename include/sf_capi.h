@@ -181,6 +181,37 @@ int sf_run_adaptive(sf_plan *plan, const int8_t *d_samples, const int16_t *d_sca
                     int32_t k_rule, float delta, int32_t shrink, int32_t *d_vis, float *d_evals,
                     float *d_evecs, int32_t *d_counts, uint16_t *d_beams_f16, void *stream);
 
+/* ---- allocation-free variant ------------------------------------------------ */
+
+/* The adaptive chain of sf_run_adaptive for callers that cannot allocate
+ * device memory: code on a real-time thread or in a host callback that must
+ * never block on the allocator, or a plugin whose host hands it pre-allocated
+ * buffers and forbids cudaMalloc.  No counterpart in the reference (its
+ * pipelines allocate their buffers in their constructors).
+ *
+ * Takes the shape and caller-owned device buffers only (no plan):
+ *   d_weights_f16  fp16 pairs [C][Pol][B][R][2]
+ *   d_factors      float pairs [C][Pol][R][2] per-receiver gain x phasor, or NULL for 1
+ *   d_delays       int32 [F] sub-packet delays in [-Tp, Tp], or NULL for 0
+ *   d_fixed_counts int32 [C] K per channel for SF_K_FIXED, or NULL for 0
+ *   d_counts       int32 [C][Pol] chosen K (may be NULL)
+ *   d_beams_f16    fp16 [C][Pol][2B][T][2] (slot 0 original, slot 1 projected)
+ *   d_status       uint32 device error bits the caller clears (may be NULL)
+ * Intermediates (visibilities, effective weights, ...) live in one 16 MiB
+ * static device array per GPU, held from first use until the process exits;
+ * shapes that need more (above about 530 channels of 36 receivers and 8 beams)
+ * return SF_ERR_UNSUPPORTED.  The first call on a device resolves that
+ * array's address (cudaGetSymbolAddress) and should come before any stream
+ * capture.  Calls share the array and keep its last contents, so calls that
+ * overlap on one GPU race: serialise them.  Allocates nothing (no cudaMalloc,
+ * cudaFree or allocating library call). */
+int sf_run_adaptive_noalloc(const sf_shape *shape, const int8_t *d_samples,
+                            const int16_t *d_scales, const uint16_t *d_weights_f16,
+                            const float *d_factors, const int32_t *d_delays,
+                            const int32_t *d_fixed_counts, int32_t k_rule, float delta,
+                            int32_t shrink, int32_t *d_counts, uint16_t *d_beams_f16,
+                            uint32_t *d_status, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

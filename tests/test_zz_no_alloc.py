@@ -1,0 +1,96 @@
+"""Allocation-free adaptive chain: sf_run_adaptive_noalloc against sf_run_adaptive.
+
+Some callers of this library cannot call cudaMalloc: a real-time thread or a
+CUDA host callback that must never block on the device allocator, or a plugin
+running inside a host application that owns all device memory and hands it
+pre-allocated buffers.  sf_run_adaptive_noalloc serves them: it takes only
+caller-owned inputs and outputs and keeps its intermediates in a fixed 16 MiB
+static device array.  These tests call it through the C ABI and check it
+against the plan-based entry point, twice in a row (the array keeps the
+previous call's contents, which must not leak into the next result).
+
+This file is collected last on purpose, so a run that stops at the first
+failure has already run every other test.
+"""
+import numpy as np
+import pytest
+import torch
+
+import sf_oracle as orc
+import sfgb
+
+pytestmark = pytest.mark.gpu
+
+SHAPE = (24, 4, 64, 36, 9, 16, 4)  # C, F, Tp, R, Rpp, P, B
+
+
+def _inputs(seed):
+    sh = orc.Shape(*SHAPE)
+    samples, scales, _ = orc.synth_inputs(sh, seed=seed, n_interferers=2, frac_channels=0.5)
+    weights = orc.synth_weights(sh, seed=seed + 10)
+    rng = np.random.default_rng(seed)
+    gains = (rng.normal(1, 0.1, (sh.C, 2, sh.R)) + 1j * rng.normal(0, 0.1, (sh.C, 2, sh.R))).astype(np.complex64)
+    delays = rng.integers(-sh.Tp, sh.Tp + 1, size=sh.F).astype(np.int32)
+    fixed = rng.integers(0, 3, size=sh.C).astype(np.int32)
+    return sh, samples, scales, weights, gains, delays, fixed
+
+
+def _plan_path(sh, samples, scales, weights, gains, delays, fixed, k_rule, delta):
+    plan = sfgb.Plan(*SHAPE)
+    plan.set_weights(weights)
+    plan.set_antenna_gains(gains)
+    plan.set_subpacket_delays(delays)
+    plan.set_fixed_counts(fixed)
+    s = torch.as_tensor(samples).cuda()
+    sc = torch.as_tensor(scales).cuda()
+    beams = torch.empty(plan.beams_shape(2), dtype=torch.float16, device="cuda")
+    cnt = torch.empty((sh.C, 2), dtype=torch.int32, device="cuda")
+    plan.run_adaptive(s, sc, k_rule, delta, False, None, None, None, cnt, beams)
+    torch.cuda.synchronize()
+    assert plan.status()[0] == 0
+    plan.close()
+    return beams.cpu().numpy().astype(np.float32), cnt.cpu().numpy()
+
+
+def _noalloc_path(sh, samples, scales, weights, gains, delays, fixed, k_rule, delta):
+    s = torch.as_tensor(samples).cuda()
+    sc = torch.as_tensor(scales).cuda()
+    w = torch.as_tensor(np.ascontiguousarray(weights)).cuda()
+    fac = torch.as_tensor(np.ascontiguousarray(np.stack([gains.real, gains.imag], -1).astype(np.float32))).cuda()
+    dl = torch.as_tensor(delays).cuda()
+    fx = torch.as_tensor(fixed).cuda()
+    beams = torch.full((sh.C, 2, 2 * sh.B, sh.T, 2), float("nan"), dtype=torch.float16, device="cuda")
+    cnt = torch.full((sh.C, 2), -1, dtype=torch.int32, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    sfgb.run_adaptive_noalloc(SHAPE, s, sc, w, k_rule, delta, False, beams, factors=fac, delays=dl,
+                              fixed_counts=fx, counts=cnt, status=status)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    return beams.cpu().numpy().astype(np.float32), cnt.cpu().numpy()
+
+
+def _close(a, b):
+    ya = a[..., 0] + 1j * a[..., 1]
+    yb = b[..., 0] + 1j * b[..., 1]
+    tol = 2.0 ** -9 * np.abs(yb) + 2.0 ** -6
+    return bool(np.all(np.abs(ya - yb) <= tol))
+
+
+def test_noalloc_matches_plan_entry_point_on_two_calls_in_a_row():
+    for seed, k_rule, delta in ((0, sfgb.SF_K_FIXED, 0.0), (1, sfgb.SF_K_DETECT, 3.0)):
+        args = _inputs(seed)
+        ref_beams, ref_counts = _plan_path(*args, k_rule, delta)
+        got_beams, got_counts = _noalloc_path(*args, k_rule, delta)
+        assert np.array_equal(got_counts, ref_counts)
+        assert _close(got_beams, ref_beams)
+
+
+def test_noalloc_rejects_shapes_beyond_its_scratch():
+    big = (4096, 4, 64, 36, 9, 16, 4)
+    s = torch.zeros(16, dtype=torch.int8, device="cuda")
+    sc = torch.zeros(16, dtype=torch.int16, device="cuda")
+    w = torch.zeros(16, dtype=torch.float16, device="cuda")
+    beams = torch.zeros(16, dtype=torch.float16, device="cuda")
+    with pytest.raises(sfgb.SfError) as ei:
+        sfgb.run_adaptive_noalloc(big, s, sc, w, sfgb.SF_K_FIXED, 0.0, False, beams)
+    assert ei.value.code == 2 and "scratch" in str(ei.value)
