@@ -115,6 +115,18 @@ SF_DEVICE void bulk_copy_g2s(void *smem_dst, const void *gmem_src, uint32_t byte
       : "memory");
 }
 
+// 4-byte asynchronous global -> shared copy, and an mbarrier arrival that
+// fires once every cp.async this thread issued before it has landed (the
+// arrival is pre-counted in the barrier's expected count).
+SF_DEVICE void cp_async4(void *smem_dst, const void *gmem_src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(smem_dst)), "l"(gmem_src)
+               : "memory");
+}
+
+SF_DEVICE void cp_async_mbar_arrive(uint64_t *bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 // ---------------------------------------------------------------------------
 // tcgen05: tensor memory and the single-thread UMMA
 // ---------------------------------------------------------------------------

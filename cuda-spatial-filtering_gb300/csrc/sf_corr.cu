@@ -17,11 +17,13 @@
 // the rest of those rows follow from V(k,m) = conj(V(m,k)).
 //
 // CTA roles (one persistent CTA per SM, 16 warps):
-//   warp 0      bulk-copy (TMA) producer: whole packets [F][Tp][Rpp][Pol][2]
-//               of a channel into a shared-memory ring
+//   warp 0      producer: one bulk (TMA) copy per packet [F][Tp][Rpp][Pol][2]
+//               of a channel into a shared-memory ring, plus the packet's
+//               int16 scales by 4-byte cp.async, both completing on the
+//               slot's mbarrier
 //   warp 1      TMEM allocation + the single-thread UMMA issuer
 //   warps 4-7   epilogue: drain fp32 chunks into int32, emit visibilities
-//   warps 8-15  converters: ring (int8) -> swizzled fp16 operand tiles,
+//   warps 2-3, 8-15  converters: ring (int8) -> swizzled fp16 operand tiles,
 //               applying the per-packet scale and the per-FPGA window offset
 #include <algorithm>
 #include <cstdio>
@@ -39,8 +41,8 @@ constexpr int NTHREADS = NUM_WARPS * 32;
 constexpr int WARP_TMA = 0;
 constexpr int WARP_MMA = 1;
 constexpr int WARP_EPI0 = 4;
-constexpr int WARP_CONV0 = 8;
-constexpr int NUM_CONV_THREADS = 8 * 32;
+constexpr int WARP_CONV0 = 8;  // converters: warps 2-3 and 8-15
+constexpr int NUM_CONV_THREADS = 10 * 32;
 constexpr int MAX_SLOTS = 32;
 constexpr int MAX_F = 64;
 constexpr uint32_t TMEM_COLS = 512;
@@ -59,7 +61,8 @@ struct CorrArgs {
   int stage_rows;  // rows per operand stage: max(NR, 128)
   int nkb;         // K blocks per channel
   int slot_bytes;  // one packet of one channel: R * Tp * 4 bytes
-  int num_slots;   // packet ring depth
+  int slot_stride; // slot_bytes + the packet's scales (R * 4 bytes), rounded to 16
+  int num_slots;   // packet ring depth (power of two)
 };
 
 struct __align__(8) Header {
@@ -127,10 +130,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
   const uint32_t stage_bytes = static_cast<uint32_t>(a.stage_rows) * 128u;
   uint8_t *ring_ptr = op_ptr + NUM_OP_STAGES * stage_bytes;
   const int NS = a.num_slots;
+  const uint32_t ns_mask = static_cast<uint32_t>(NS - 1);
+  const uint32_t ns_shift = __popc(ns_mask);
 
   if (tid == 0) {
     for (int s = 0; s < NS; ++s) {
-      mbar_init(&h.pk_full[s], 1);
+      mbar_init(&h.pk_full[s], 1 + 32);
       mbar_init(&h.pk_empty[s], 1);
     }
     for (int s = 0; s < NUM_OP_STAGES; ++s) {
@@ -173,27 +178,35 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
   volatile int *abort_flag = &h.abort;
 
   if (warp == WARP_TMA) {
-    // ---------------- bulk-copy producer ----------------
-    if (lane == 0) {
-      uint32_t g = 0;
-      bool stop = false;
-      for (int c = blockIdx.x; c < a.C && !stop; c += gridDim.x) {
-        const int8_t *chan = a.samples + (size_t)c * (a.P + 2) * a.slot_bytes;
-        for (int q = qa0; q <= qbN; ++q) {
-          const uint32_t slot = g % NS;
-          if (!mbar_wait(&h.pk_empty[slot], ((g / NS) & 1u) ^ 1u, abort_flag)) {
-            stop = true;
-            break;
-          }
-          mbar_arrive_expect_tx(&h.pk_full[slot], a.slot_bytes);
-          bulk_copy_g2s(ring_ptr + (size_t)slot * a.slot_bytes, chan + (size_t)q * a.slot_bytes,
-                        a.slot_bytes, &h.pk_full[slot]);
-          ++g;
+    // ---------------- producer (whole warp) ----------------
+    uint32_t g = 0;
+    bool stop = false;
+    for (int c = blockIdx.x; c < a.C && !stop; c += gridDim.x) {
+      const int8_t *chan = a.samples + (size_t)c * (a.P + 2) * a.slot_bytes;
+      const int16_t *chan_sc = a.scales + (size_t)c * (a.P + 2) * R * 2;
+      for (int q = qa0; q <= qbN; ++q) {
+        const uint32_t slot = g & ns_mask;
+        const bool ok = mbar_wait(&h.pk_empty[slot], ((g >> ns_shift) & 1u) ^ 1u, abort_flag);
+        if (__any_sync(0xffffffffu, !ok)) {
+          stop = true;
+          break;
         }
+        uint8_t *dst = ring_ptr + (size_t)slot * a.slot_stride;
+        if (lane == 0) {
+          mbar_arrive_expect_tx(&h.pk_full[slot], a.slot_bytes);
+          bulk_copy_g2s(dst, chan + (size_t)q * a.slot_bytes, a.slot_bytes, &h.pk_full[slot]);
+        }
+        const uint32_t *src_sc = reinterpret_cast<const uint32_t *>(chan_sc + (size_t)q * R * 2);
+        uint32_t *dst_sc = reinterpret_cast<uint32_t *>(dst + a.slot_bytes);
+        for (int r = lane; r < R; r += 32) cp_async4(dst_sc + r, src_sc + r);
+        cp_async_mbar_arrive(&h.pk_full[slot]);
+        ++g;
       }
-      // Every issued copy lands before shared memory is released.
+    }
+    // Every issued copy lands before shared memory is released.
+    if (lane == 0) {
       const uint32_t first = g > (uint32_t)NS ? g - NS : 0u;
-      for (uint32_t gq = first; gq < g; ++gq) mbar_wait_drain(&h.pk_full[gq % NS], (gq / NS) & 1u);
+      for (uint32_t gq = first; gq < g; ++gq) mbar_wait_drain(&h.pk_full[gq & ns_mask], (gq >> ns_shift) & 1u);
       if (stop) atomicOr(a.status, SF_DEVERR_TIMEOUT_TMA);
     }
   } else if (warp == WARP_MMA) {
@@ -304,14 +317,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
       }
     }
     if (failed && lane == 0) atomicOr(a.status, SF_DEVERR_TIMEOUT_EPILOGUE);
-  } else if (warp >= WARP_CONV0) {
+  } else if (warp >= WARP_CONV0 || warp == 2 || warp == 3) {
     // ---------------- converters ----------------
-    const int ct = tid - WARP_CONV0 * 32;
+    const int ct = warp >= WARP_CONV0 ? (warp - WARP_CONV0 + 2) * 32 + lane : (warp - 2) * 32 + lane;
     uint32_t g_base = 0, op_iter = 0;
     bool failed = false;
+    const int Rpp4 = a.Rpp * 4;
     for (int c = blockIdx.x; c < a.C; c += gridDim.x) {
       int q_rel = qa0;
-      const int16_t *chan_scales = a.scales + (size_t)c * (a.P + 2) * R * 2;
       for (int kb = 0; kb < a.nkb; ++kb) {
         const int s0 = kb * KBLK;
         const int s1 = min(s0 + KBLK - 1, T - 1);
@@ -320,7 +333,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
         bool ok = true;
         for (int q = qa; q <= qb && ok; ++q) {
           const uint32_t gq = g_base + (q - qa0);
-          ok = mbar_wait(&h.pk_full[gq % NS], (gq / NS) & 1u, abort_flag);
+          ok = mbar_wait(&h.pk_full[gq & ns_mask], (gq >> ns_shift) & 1u, abort_flag);
         }
         const uint32_t st = op_iter % NUM_OP_STAGES;
         ok = ok && mbar_wait(&h.op_empty[st], ((op_iter / NUM_OP_STAGES) & 1u) ^ 1u, abort_flag);
@@ -332,32 +345,37 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
             const int r = task >> 3;
             const int f = r / a.Rpp;
             const int n = r - f * a.Rpp;
-            const int off = h.offsets[f];
+            const int sfirst = s0 + oct * 8;
+            // packet / time of the first sample, then step forward
+            int qq = sfirst + h.offsets[f];
+            int pkt = qq / Tp;
+            int tt = qq - pkt * Tp;
+            const uint8_t *slot_ptr = ring_ptr + (size_t)((g_base + (pkt - qa0)) & ns_mask) * a.slot_stride;
+            uint32_t scw = *reinterpret_cast<const uint32_t *>(slot_ptr + a.slot_bytes + r * 4);
+            const uint8_t *src = slot_ptr + (f * Tp + tt) * Rpp4 + n * 4;
             uint32_t col[4][4];  // [row: p0re, p0im, p1re, p1im][pair of samples]
-            int last_pkt = -1;
-            uint32_t scw = 0;
 #pragma unroll
             for (int e = 0; e < 8; e += 2) {
               __half2 v0[2], v1[2];
 #pragma unroll
-              for (int d = 0; d < 2; ++d) {
-                const int s = s0 + oct * 8 + e + d;
-                uint32_t word = 0;
-                uint32_t sc = 0;
-                if (s < T) {
-                  const int qq = s + off;
-                  const int pkt = qq / Tp;
-                  const int tt = qq - pkt * Tp;
-                  const uint32_t slot = (g_base + (pkt - qa0)) % NS;
-                  word = *reinterpret_cast<const uint32_t *>(
-                      ring_ptr + (size_t)slot * a.slot_bytes + ((f * Tp + tt) * a.Rpp + n) * 4);
-                  if (pkt != last_pkt) {
-                    scw = __ldg(reinterpret_cast<const uint32_t *>(chan_scales + ((size_t)pkt * R + r) * 2));
-                    last_pkt = pkt;
-                  }
+              for (int dd = 0; dd < 2; ++dd) {
+                uint32_t word = 0, sc = 0;
+                if (sfirst + e + dd < T) {
+                  word = *reinterpret_cast<const uint32_t *>(src);
                   sc = scw;
                 }
-                convert_word(word, sc, v0[d], v1[d]);
+                convert_word(word, sc, v0[dd], v1[dd]);
+                // advance one sample (crossing into the next packet's slot if needed)
+                if (++tt == Tp) {
+                  tt = 0;
+                  ++pkt;
+                  slot_ptr = ring_ptr + (size_t)((g_base + (pkt - qa0)) & ns_mask) * a.slot_stride;
+                  if (sfirst + e + dd + 1 < T)
+                    scw = *reinterpret_cast<const uint32_t *>(slot_ptr + a.slot_bytes + r * 4);
+                  src = slot_ptr + (f * Tp) * Rpp4 + n * 4;
+                } else {
+                  src += Rpp4;
+                }
               }
               col[0][e >> 1] = __byte_perm(u32_of(v0[0]), u32_of(v0[1]), 0x5410);
               col[1][e >> 1] = __byte_perm(u32_of(v0[0]), u32_of(v0[1]), 0x7632);
@@ -381,7 +399,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
           const int next = (kb + 1 < a.nkb) ? ((kb + 1) * KBLK + off_min) / Tp : qbN + 1;
           for (; q_rel < next; ++q_rel) {
             const uint32_t gq = g_base + (q_rel - qa0);
-            mbar_arrive(&h.pk_empty[gq % NS]);
+            mbar_arrive(&h.pk_empty[gq & ns_mask]);
           }
         }
         ++op_iter;
@@ -435,6 +453,7 @@ cudaError_t sf_launch_correlate(const sf_plan *p, const int8_t *samples, const i
   a.stage_rows = std::max(a.NR, 128);
   a.nkb = (p->T + KBLK - 1) / KBLK;
   a.slot_bytes = p->R * p->Tp * 4;
+  a.slot_stride = a.slot_bytes + ((p->R * 4 + 15) / 16) * 16;
 
   if (!g_max_smem) {
     int dev = 0;
@@ -444,10 +463,11 @@ cudaError_t sf_launch_correlate(const sf_plan *p, const int8_t *samples, const i
   const size_t fixed = HEADER_BYTES + 1024 + (size_t)NUM_OP_STAGES * a.stage_rows * 128;
   const int need_slots = 63 / p->Tp + 5;
   long avail = (long)g_max_smem - (long)fixed;
-  int ns = avail > 0 ? (int)std::min<long>(MAX_SLOTS, avail / a.slot_bytes) : 0;
+  int ns = avail > 0 ? (int)std::min<long>(MAX_SLOTS, avail / a.slot_stride) : 0;
+  while (ns & (ns - 1)) ns &= ns - 1;  // round down to a power of two
   if (ns < need_slots) return cudaErrorInvalidConfiguration;
   a.num_slots = ns;
-  const size_t smem = fixed + (size_t)ns * a.slot_bytes;
+  const size_t smem = fixed + (size_t)ns * a.slot_stride;
   if (!g_attr_set) {
     cudaError_t e = cudaFuncSetAttribute(sf_corr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          g_max_smem);

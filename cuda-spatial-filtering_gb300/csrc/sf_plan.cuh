@@ -46,6 +46,11 @@ cudaError_t sf_launch_eig(const sf_plan *p, const int32_t *vis, int eig_mode, in
                           __half2 *proj, cudaStream_t stream);
 int sf_eig_supported(const sf_plan *p, char *why, size_t why_len);
 
+size_t sf_eig_topk_smem(int n, int B);
+int sf_eig_topk_supported(const sf_plan *p);
+cudaError_t sf_launch_eig_topk(const sf_plan *p, const int32_t *vis, int k_rule, float delta, int shrink,
+                               float *evals, int32_t *counts, cudaStream_t stream);
+
 cudaError_t sf_launch_weights_plain(const sf_plan *p, cudaStream_t stream);
 cudaError_t sf_launch_beam(const sf_plan *p, const int8_t *samples, const int16_t *scales,
                            const int32_t *offsets, int n_slots, __half2 *beams,

@@ -145,7 +145,7 @@ def test_correlator_many_channels_persistent_loop():
 # Eigensolver, projector, beams on LAMBDA-shaped synthetic data
 # --------------------------------------------------------------------------
 def _run_adaptive_gpu(sh, samples, scales, weights, k_rule, delta, shrink=False, fixed=None,
-                      gains=None, fine=None):
+                      gains=None, fine=None, want_evecs=True):
     plan = sfgb.Plan(sh.C, sh.F, sh.Tp, sh.R, sh.Rpp, sh.P, sh.B)
     plan.set_weights(weights)
     if fixed is not None:
@@ -161,14 +161,15 @@ def _run_adaptive_gpu(sh, samples, scales, weights, k_rule, delta, shrink=False,
     vec = torch.empty((sh.C, 2, sh.R, sh.R, 2), dtype=torch.float32, device="cuda")
     cnt = torch.empty((sh.C, 2), dtype=torch.int32, device="cuda")
     beams = torch.empty(plan.beams_shape(2), dtype=torch.float16, device="cuda")
-    plan.run_adaptive(s, sc, k_rule, delta, shrink, vis, ev, vec, cnt, beams)
+    plan.run_adaptive(s, sc, k_rule, delta, shrink, vis, ev, vec if want_evecs else None, cnt, beams)
     torch.cuda.synchronize()
     rc, bits = plan.status()
     assert rc == 0 and bits == 0, f"device status 0x{bits:x}"
     out = {"vis": vis.cpu().numpy(), "evals": ev.cpu().numpy(), "counts": cnt.cpu().numpy(),
            "beams": beams.cpu().numpy().astype(np.float32)}
-    v = vec.cpu().numpy()
-    out["evecs"] = v[..., 0] + 1j * v[..., 1]
+    if want_evecs:
+        v = vec.cpu().numpy()
+        out["evecs"] = v[..., 0] + 1j * v[..., 1]
     plan.close()
     return out
 
@@ -269,3 +270,71 @@ def test_gains_and_fine_delays_folded(lambda_cfg):
     yb = got["beams"][..., 0] + 1j * got["beams"][..., 1]
     tol = 2.0 ** -9 * np.abs(yr) + 2.0 ** -6 + 2e-3 * np.abs(yr).max(axis=-1, keepdims=True)
     assert np.all(np.abs(yb - yr) <= tol)
+
+
+# --------------------------------------------------------------------------
+# Top-K eigensolver (tridiagonal + bisection + inverse iteration): the path the
+# adaptive chain takes when no eigenvector output is requested
+# --------------------------------------------------------------------------
+def _beams_close(got, ref_beams, rel_peak=1e-3):
+    yb = got[..., 0] + 1j * got[..., 1]
+    tol = 2.0 ** -9 * np.abs(ref_beams) + 2.0 ** -6 + rel_peak * np.abs(ref_beams).max(axis=-1, keepdims=True)
+    return np.abs(yb - ref_beams) <= tol
+
+
+@pytest.mark.parametrize("shrink", [False, True])
+def test_topk_path_eigenvalues_and_beams(lambda_cfg, shrink):
+    sh, samples, scales, weights, rfi = lambda_cfg
+    fixed = np.full(sh.C, 2)
+    got = _run_adaptive_gpu(sh, samples, scales, weights, sfgb.SF_K_FIXED, 0.0, shrink=shrink, fixed=fixed,
+                            want_evecs=False)
+    ref = orc.adaptive_chain(sh, samples, scales, weights, k_fixed=fixed, shrink=shrink)
+    vc = orc.scaled_visibilities(sh, ref["vis"], orc.receiver_factors(sh))
+    for p in range(2):
+        m = orc.unpack_hermitian(sh, vc, p, p)
+        for c in range(sh.C):
+            a, _ = orc.whiten(m[c])
+            norm = np.linalg.norm(a, 2)
+            assert np.max(np.abs(got["evals"][c, p] - ref["evals"][c, p])) <= 2e-5 * norm
+    ok = _beams_close(got["beams"], ref["beams"])
+    assert ok.all(), f"{(~ok).sum()} beam samples outside tolerance"
+
+
+def test_topk_path_matches_jacobi_path(lambda_cfg):
+    sh, samples, scales, weights, rfi = lambda_cfg
+    fixed = np.full(sh.C, 3)
+    a = _run_adaptive_gpu(sh, samples, scales, weights, sfgb.SF_K_FIXED, 0.0, fixed=fixed, want_evecs=False)
+    b = _run_adaptive_gpu(sh, samples, scales, weights, sfgb.SF_K_FIXED, 0.0, fixed=fixed, want_evecs=True)
+    ya = a["beams"][..., 0] + 1j * a["beams"][..., 1]
+    assert _beams_close(b["beams"], ya, rel_peak=2e-3).all()
+
+
+def test_topk_path_detection(lambda_cfg):
+    sh, samples, scales, weights, rfi = lambda_cfg
+    got = _run_adaptive_gpu(sh, samples, scales, weights, sfgb.SF_K_DETECT, 3.0, want_evecs=False)
+    for c in range(sh.C):
+        for p in range(2):
+            assert got["counts"][c, p] == orc.detect_k_f32(got["evals"][c, p], 3.0)
+    assert np.all(got["counts"][rfi] >= 2)
+    ref = orc.adaptive_chain(sh, samples, scales, weights, detect=True, delta=3.0)
+    ok = _beams_close(got["beams"], ref["beams"])
+    # channels whose K agrees with the FP64 oracle must agree in their beams
+    same = got["counts"] == ref["counts"]
+    assert ok[same].all()
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c.path == "adaptive"],
+                         ids=[c.name for c in CASES if c.path == "adaptive"])
+def test_reference_adaptive_goldens_topk_path(case):
+    sh = oracle_shape(case)
+    a = case.adaptive
+    rule = sfgb.SF_K_DETECT if a.get("detect") else sfgb.SF_K_FIXED
+    got = _run_adaptive_gpu(sh, case.samples, case.scales, case.weights, rule, a.get("delta", 3.0),
+                            shrink=a.get("shrink", False), fixed=np.full(sh.C, a.get("k", 0)),
+                            want_evecs=False)
+    out = {"beam_half": got["beams"], "counts": got["counts"], "evals": got["evals"]}
+    e = dict(case.expect)
+    import copy
+    c2 = copy.copy(case)
+    c2.expect = {k: v for k, v in e.items() if k not in ("evals", "principal_evec")}
+    check_case(c2, out)
