@@ -167,6 +167,9 @@ cudaError_t sf_launch_beam(const sf_plan *p, const int8_t *samples, const int16_
   a.B = p->B;
   a.NB = n_slots * p->B;
   a.NBW = 2 * p->B;
+  // The tensor-core beamformer (sf_corr.cu) serves every shape it supports.
+  if (sf_beam_tc_supported(p, a.NB))
+    return sf_launch_corrbeam(p, samples, scales, offsets, nullptr, a.NB, beams, 2, stream);
   if (a.NB <= 1) return launch_beam_t<1>(a, stream);
   if (a.NB <= 2) return launch_beam_t<2>(a, stream);
   if (a.NB <= 4) return launch_beam_t<4>(a, stream);

@@ -351,6 +351,18 @@ int sf_run_corr_beam(sf_plan *plan, const int8_t *d_samples, const int16_t *d_sc
                      int32_t *d_vis, uint16_t *d_beams_f16, void *stream) {
   if (int rc = check_plan(plan)) return rc;
   int32_t *vis = d_vis ? d_vis : plan->d_vis;
+  if (!d_samples || !d_scales || !d_beams_f16) return set_err(SF_ERR_INVALID_ARGUMENT, "NULL buffer");
+  char why[160];
+  if (sf_correlate_supported(plan, why, sizeof(why)) && sf_beam_tc_supported(plan, plan->B) &&
+      reinterpret_cast<uintptr_t>(d_samples) % 16 == 0) {
+    // one pass over the samples: correlation and beams from the same tiles
+    cudaStream_t s = as_stream(stream);
+    SF_TRY(sf_launch_weights_plain(plan, s), "weights launch");
+    SF_TRY(sf_launch_corrbeam(plan, d_samples, d_scales, plan->d_off_packet, vis, plan->B,
+                              reinterpret_cast<__half2 *>(d_beams_f16), 3, s),
+           "correlate+beamform launch");
+    return SF_OK;
+  }
   if (int rc = sf_correlate(plan, d_samples, d_scales, SF_WINDOW_PACKET, vis, stream)) return rc;
   return sf_beamform(plan, d_samples, d_scales, SF_WINDOW_PACKET, 1, d_beams_f16, stream);
 }
@@ -361,6 +373,18 @@ int sf_run_lambda_gpu(sf_plan *plan, const int8_t *d_samples, const int16_t *d_s
   if (int rc = check_plan(plan)) return rc;
   int32_t *vis = d_vis ? d_vis : plan->d_vis;
   float *evals = d_evals ? d_evals : plan->d_evals;
+  if (!d_samples || !d_scales || !d_beams_f16) return set_err(SF_ERR_INVALID_ARGUMENT, "NULL buffer");
+  char why[160];
+  if (sf_correlate_supported(plan, why, sizeof(why)) && sf_beam_tc_supported(plan, plan->B) &&
+      reinterpret_cast<uintptr_t>(d_samples) % 16 == 0) {
+    cudaStream_t s = as_stream(stream);
+    SF_TRY(sf_launch_weights_plain(plan, s), "weights launch");
+    SF_TRY(sf_launch_corrbeam(plan, d_samples, d_scales, plan->d_off_aligned, vis, plan->B,
+                              reinterpret_cast<__half2 *>(d_beams_f16), 3, s),
+           "correlate+beamform launch");
+    return sf_covariance_eig(plan, vis, SF_EIG_ALL_BLOCKS, SF_K_FIXED, 0.f, 0, evals, d_evecs, nullptr,
+                             nullptr, stream);
+  }
   if (int rc = sf_correlate(plan, d_samples, d_scales, SF_WINDOW_ALIGNED, vis, stream)) return rc;
   if (int rc = sf_covariance_eig(plan, vis, SF_EIG_ALL_BLOCKS, SF_K_FIXED, 0.f, 0, evals, d_evecs,
                                  nullptr, nullptr, stream))

@@ -67,12 +67,15 @@ SF_DEVICE bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 
 // Wait for the phase with the given parity to complete.  Returns false (and
 // raises *abort) when SF_WAIT_CYCLES clock cycles pass or another role has
-// already aborted, so no thread of the CTA can spin forever.
-SF_DEVICE bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort) {
+// already aborted, so no thread of the CTA can spin forever.  Roles that wait
+// long (producer, epilogue) pass a sleep between polls so their spinning does
+// not take issue slots from the converter warps.
+SF_DEVICE bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort, uint32_t sleep_ns = 0) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   uint32_t n = 0;
   while (!mbar_try_wait(bar, parity)) {
+    if (sleep_ns) __nanosleep(sleep_ns);
     if ((++n & 63u) == 0) {
       if (*abort) return false;
       if (clock64() - t0 > SF_WAIT_CYCLES) {

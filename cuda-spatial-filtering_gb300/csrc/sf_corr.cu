@@ -1,30 +1,39 @@
-// Tensor-core correlator: one integration of int8 complex voltages in the
-// packet layout -> exact int32 visibilities in the trimmed packed-triangle
-// layout.  Replaces the reference's fp16 conversion + layout permutations +
-// Tensor Core Correlator + trim (include/spatial/spatial.cuh:55-304,
-// include/spatial/pipeline/lambda_gpu_pipeline.hpp:640-671, src/spatial.cu:176-200).
+// Tensor-core correlator and beamformer over one integration of int8 complex
+// voltages in the packet layout.
 //
-// Per channel the kernel forms the real Gram matrix G = A A^T of the stacked
-// real/imaginary rows of all receivers and polarisations (row u = 2k + comp,
-// k = pol * R + receiver) with tcgen05 UMMA, fp16 operands and fp32
-// accumulation in tensor memory.  The int8 x int16-scale products are exact in
-// fp16 (|x s| <= 2048) and every 512-sample chunk of fp32 partial sums is exact
-// (|sum| <= 512 * 2 * 128^2 = 2^24), so each chunk is drained into int32
-// running sums held in tensor memory; the visibilities come out bit-exact.
-//   Re V(k,m) = G[2k][2m] + G[2k+1][2m+1],  Im V(k,m) = G[2k+1][2m] - G[2k][2m+1]
-// Rows 0..127 of G come from one M=128 x N=NR MMA; when NR > 128 the rows
-// 128..NR-1 x columns 128..NR-1 come from a second M=128 x N=NR-128 MMA and
-// the rest of those rows follow from V(k,m) = conj(V(m,k)).
+// One persistent CTA per SM streams each channel's packets once through
+// shared memory and builds fp16 operand tiles A[u][t] (row u = 2k + comp,
+// k = pol * R + receiver; 64 samples t per 128-byte row, 128-byte swizzle).
+// From the same tiles it can
+//   * correlate: G = A A^T with tcgen05 UMMA (A K-major), fp32 accumulation in
+//     tensor memory, drained every 512 samples into int32 running sums -> exact
+//     int32 visibilities in the trimmed packed-triangle layout.  Replaces the
+//     reference's fp16 ingest + layout permutations + Tensor Core Correlator +
+//     trim (include/spatial/spatial.cuh:55-304, lambda_gpu_pipeline.hpp:640-671,
+//     src/spatial.cu:176-200).
+//       Re V(k,m) = G[2k][2m] + G[2k+1][2m+1],  Im V(k,m) = G[2k+1][2m] - G[2k][2m+1]
+//     Rows 0..127 of G come from one M=128 x N=NR MMA; rows 128..NR-1 x columns
+//     128..NR-1 from a second M=128 x N=NR-128 MMA; the rest is V(k,m) = conj(V(m,k)).
+//   * beamform: Y^T[t][n] = sum_u A^T[t][u] W[n][u] per 128 samples, A read
+//     MN-major (two 64-sample tiles side by side), W the block-diagonal real
+//     form of the effective weights (n = pol, beam, re/im), fp32 accumulation,
+//     fp16 output [C][Pol][NB][T][2].  Replaces the reference's
+//     col-major sample layout + weight permutation + ccglib GEMM + half output
+//     (spatial.cuh:145-213, 376-418; lambda_gpu_pipeline.hpp:708-743).
+//   * or both in one pass (the plain pipelines).
+// Operands: fp16(x * scale) is exact for |x s| <= 2048 and equals the
+// reference's ingest for unit gain; correlation chunks are exact while
+// |partial sums| <= 2^24 (512 samples of |x s| <= 128).
 //
-// CTA roles (one persistent CTA per SM, 16 warps):
-//   warp 0      producer: one bulk (TMA) copy per packet [F][Tp][Rpp][Pol][2]
-//               of a channel into a shared-memory ring, plus the packet's
-//               int16 scales by 4-byte cp.async, both completing on the
-//               slot's mbarrier
-//   warp 1      TMEM allocation + the single-thread UMMA issuer
-//   warps 4-7   epilogue: drain fp32 chunks into int32, emit visibilities
-//   warps 2-3, 8-15  converters: ring (int8) -> swizzled fp16 operand tiles,
-//               applying the per-packet scale and the per-FPGA window offset
+// CTA roles (16 warps):
+//   warp 0           producer: one bulk (TMA) copy per packet [F][Tp][Rpp][Pol][2]
+//                    plus the packet's scales by 4-byte cp.async, completing on
+//                    the slot's mbarrier
+//   warp 1           TMEM allocation + the single-thread UMMA issuer
+//   warps 4-7        epilogue (one TMEM lane quarter each)
+//   warps 2-3, 8-15  converters: ring (int8) -> swizzled fp16 tiles (per-packet
+//                    scale, per-FPGA window offset); per channel the weight tile
+// Every wait is bounded (about a second) and reports through the status word.
 #include <algorithm>
 #include <cstdio>
 
@@ -45,24 +54,30 @@ constexpr int WARP_CONV0 = 8;  // converters: warps 2-3 and 8-15
 constexpr int NUM_CONV_THREADS = 10 * 32;
 constexpr int MAX_SLOTS = 32;
 constexpr int MAX_F = 64;
-constexpr uint32_t TMEM_COLS = 512;
-constexpr uint32_t TMEM_I32 = 256;   // column offset of the int32 running sums
 constexpr uint32_t HEADER_BYTES = 2048;
-constexpr int MAX_R = 48;            // NR + (NR - 128) <= 256 tensor-memory columns
+constexpr int MAX_R = 48;
+constexpr int MAX_BEAM_OUT = 16;  // beams (all slots) per pol in the tensor beamformer
 
 struct CorrArgs {
   const int8_t *samples;
   const int16_t *scales;
   const int32_t *offsets;
   int32_t *vis;
+  const float2 *weff;  // [C][2][NBW][R]
+  __half2 *beams;      // [C][2][NB][T]
   uint32_t *status;
   int C, F, Tp, R, Rpp, P, T, NBL;
-  int NR;          // operand rows holding data: round_up(4R, 16)
-  int stage_rows;  // rows per operand stage: max(NR, 128)
-  int nkb;         // K blocks per channel
-  int slot_bytes;  // one packet of one channel: R * Tp * 4 bytes
-  int slot_stride; // slot_bytes + the packet's scales (R * 4 bytes), rounded to 16
-  int num_slots;   // packet ring depth (power of two)
+  int NR;           // operand rows holding data: round_up(4R, 16)
+  int stage_rows;   // rows per operand stage: max(NR, 128)
+  int nkb;          // K blocks per channel (even when beamforming)
+  int slot_bytes;   // one packet of one channel: R * Tp * 4 bytes
+  int slot_stride;  // slot_bytes + the packet's scales, rounded to 16
+  int num_slots;    // packet ring depth (power of two)
+  int NB, NBW;      // beams written per pol; rows of weff per (c, p)
+  int BN;           // beam MMA N = round_up(4 NB, 16)
+  int katoms;       // 64-column K atoms of the weight tile: ceil(NR / 64)
+  uint32_t wtile_bytes;
+  uint32_t tmem_cols, i32_off, beam_off;
 };
 
 struct __align__(8) Header {
@@ -72,6 +87,10 @@ struct __align__(8) Header {
   uint64_t op_empty[NUM_OP_STAGES];
   uint64_t acc_full;
   uint64_t acc_empty;
+  uint64_t beam_full[2];
+  uint64_t beam_empty[2];
+  uint64_t w_full[2];
+  uint64_t w_empty[2];
   uint64_t mma_done;
   uint32_t tmem_base;
   int abort;
@@ -90,21 +109,23 @@ __device__ __forceinline__ void convert_word(uint32_t word, uint32_t scw, __half
   // 0x6400 | b is the fp16 value 1024 + b, exact for b in [0, 1023]
   const __half2 h01 = h2_of(__byte_perm(biased, 0x64646464u, 0x4140));
   const __half2 h23 = h2_of(__byte_perm(biased, 0x64646464u, 0x4342));
-  const __half2 bias = __floats2half2_rn(1152.0f, 1152.0f);
-  __half2 x01 = __hsub2(h01, bias);  // exact integers in [-128, 127]
+  const __half2 bias = h2_of(0x64806480u);  // 1152
+  __half2 x01 = __hsub2(h01, bias);         // exact integers in [-128, 127]
   __half2 x23 = __hsub2(h23, bias);
-  const int s0 = static_cast<int16_t>(scw & 0xFFFFu);
-  const int s1 = static_cast<int16_t>(scw >> 16);
-  if (s0 >= -2048 && s0 <= 2048 && s1 >= -2048 && s1 <= 2048) {
-    // both factors exact in fp16: one correctly rounded product, as the
-    // reference's int multiply + float->half conversion
-    x01 = __hmul2(x01, __half2half2(__int2half_rn(s0)));
-    x23 = __hmul2(x23, __half2half2(__int2half_rn(s1)));
-  } else {
-    const int a0 = static_cast<int8_t>(word & 0xFF), a1 = static_cast<int8_t>((word >> 8) & 0xFF);
-    const int a2 = static_cast<int8_t>((word >> 16) & 0xFF), a3 = static_cast<int8_t>(word >> 24);
-    x01 = __floats2half2_rn(static_cast<float>(a0 * s0), static_cast<float>(a1 * s0));
-    x23 = __floats2half2_rn(static_cast<float>(a2 * s1), static_cast<float>(a3 * s1));
+  if (scw != 0x00010001u) {
+    const int s0 = static_cast<int16_t>(scw & 0xFFFFu);
+    const int s1 = static_cast<int16_t>(scw >> 16);
+    if (s0 >= -2048 && s0 <= 2048 && s1 >= -2048 && s1 <= 2048) {
+      // both factors exact in fp16: one correctly rounded product, as the
+      // reference's int multiply + float->half conversion
+      x01 = __hmul2(x01, __half2half2(__int2half_rn(s0)));
+      x23 = __hmul2(x23, __half2half2(__int2half_rn(s1)));
+    } else {
+      const int a0 = static_cast<int8_t>(word & 0xFF), a1 = static_cast<int8_t>((word >> 8) & 0xFF);
+      const int a2 = static_cast<int8_t>((word >> 16) & 0xFF), a3 = static_cast<int8_t>(word >> 24);
+      x01 = __floats2half2_rn(static_cast<float>(a0 * s0), static_cast<float>(a1 * s0));
+      x23 = __floats2half2_rn(static_cast<float>(a2 * s1), static_cast<float>(a3 * s1));
+    }
   }
   p0 = x01;
   p1 = x23;
@@ -112,12 +133,23 @@ __device__ __forceinline__ void convert_word(uint32_t word, uint32_t scw, __half
 
 __device__ __forceinline__ void emit_vis(const CorrArgs &a, int c, int p, int i, int q, int j,
                                          int comp, int val) {
-  const size_t idx =
-      ((((size_t)c * a.NBL + baseline_of(i, j)) * 2 + p) * 2 + q) * 2 + comp;
+  const size_t idx = ((((size_t)c * a.NBL + baseline_of(i, j)) * 2 + p) * 2 + q) * 2 + comp;
   a.vis[idx] = val;
 }
 
-__global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) {
+// Shared-memory descriptor with explicit strides (128-byte swizzle).
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((addr >> 4) & 0x3FFFu);
+  d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFFu) << 16;
+  d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFFu) << 32;
+  d |= static_cast<uint64_t>(1u) << 46;
+  d |= static_cast<uint64_t>(2u) << 61;
+  return d;
+}
+
+template <bool DO_CORR, bool DO_BEAM>
+__global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   Header &h = *reinterpret_cast<Header *>(smem);
   const int tid = threadIdx.x;
@@ -128,7 +160,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
   const uint32_t op_addr = (sbase + HEADER_BYTES + 1023u) & ~1023u;
   uint8_t *op_ptr = smem + (op_addr - sbase);
   const uint32_t stage_bytes = static_cast<uint32_t>(a.stage_rows) * 128u;
-  uint8_t *ring_ptr = op_ptr + NUM_OP_STAGES * stage_bytes;
+  const uint32_t w_addr = op_addr + NUM_OP_STAGES * stage_bytes;  // weight tiles (1024-aligned)
+  uint8_t *w_ptr = op_ptr + NUM_OP_STAGES * stage_bytes;
+  uint8_t *ring_ptr = w_ptr + (DO_BEAM ? 2 * a.wtile_bytes : 0u);
   const int NS = a.num_slots;
   const uint32_t ns_mask = static_cast<uint32_t>(NS - 1);
   const uint32_t ns_shift = __popc(ns_mask);
@@ -144,21 +178,26 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
     }
     mbar_init(&h.acc_full, 1);
     mbar_init(&h.acc_empty, 4);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&h.beam_full[b], 1);
+      mbar_init(&h.beam_empty[b], 4);
+      mbar_init(&h.w_full[b], 1);
+      mbar_init(&h.w_empty[b], 1);
+    }
     mbar_init(&h.mma_done, 1);
     h.abort = 0;
     fence_mbarrier_init();
   }
   for (int f = tid; f < a.F; f += NTHREADS) h.offsets[f] = a.offsets[f];
-  // Padding rows of the operand tiles must read as zero; data rows are
-  // rewritten for every K block.
+  // Padding rows/columns of the operand and weight tiles must read as zero.
   {
     uint4 *z = reinterpret_cast<uint4 *>(op_ptr);
-    const int n16 = NUM_OP_STAGES * stage_bytes / 16;
+    const int n16 = (NUM_OP_STAGES * stage_bytes + (DO_BEAM ? 2 * a.wtile_bytes : 0u)) / 16;
     for (int i = tid; i < n16; i += NTHREADS) z[i] = make_uint4(0, 0, 0, 0);
     fence_proxy_async_smem();
   }
   if (warp == WARP_MMA) {
-    tmem_alloc(&h.tmem_base, TMEM_COLS);
+    tmem_alloc(&h.tmem_base, a.tmem_cols);
     tmem_relinquish();
   }
   tc_fence_before();
@@ -186,7 +225,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
       const int16_t *chan_sc = a.scales + (size_t)c * (a.P + 2) * R * 2;
       for (int q = qa0; q <= qbN; ++q) {
         const uint32_t slot = g & ns_mask;
-        const bool ok = mbar_wait(&h.pk_empty[slot], ((g >> ns_shift) & 1u) ^ 1u, abort_flag);
+        const bool ok = mbar_wait(&h.pk_empty[slot], ((g >> ns_shift) & 1u) ^ 1u, abort_flag, 64);
         if (__any_sync(0xffffffffu, !ok)) {
           stop = true;
           break;
@@ -217,36 +256,66 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
       const bool corner = NR > 128;
       const uint32_t idesc_main = umma_idesc_f16_f32(128, NR);
       const uint32_t idesc_corner = umma_idesc_f16_f32(128, corner ? NR - 128 : 16);
-      uint32_t op_iter = 0, acc_iter = 0;
+      // beam: A (samples) MN-major, B (weights) K-major, M = 128 samples, N = BN
+      const uint32_t idesc_beam = umma_idesc_f16_f32(128, a.BN) | (1u << 15);
+      uint32_t op_iter = 0, acc_iter = 0, beam_iter = 0, cw = 0;
       bool failed = false;
-      for (int c = blockIdx.x; c < a.C; c += gridDim.x) {
+      for (int c = blockIdx.x; c < a.C; c += gridDim.x, ++cw) {
+        const uint32_t wb = cw & 1u;
+        if (DO_BEAM) failed |= !mbar_wait(&h.w_full[wb], (cw >> 1) & 1u, abort_flag);
         for (int kb = 0; kb < a.nkb; ++kb) {
           const uint32_t st = op_iter % NUM_OP_STAGES;
           bool ok = mbar_wait(&h.op_full[st], (op_iter / NUM_OP_STAGES) & 1u, abort_flag);
           const bool chunk_start = (kb % CHUNK_KBLK) == 0;
-          if (chunk_start) ok = mbar_wait(&h.acc_empty, (acc_iter & 1u) ^ 1u, abort_flag) && ok;
+          if (DO_CORR && chunk_start) ok = mbar_wait(&h.acc_empty, (acc_iter & 1u) ^ 1u, abort_flag) && ok;
+          const bool beam_now = DO_BEAM && (kb & 1);
+          if (beam_now)
+            ok = mbar_wait(&h.beam_empty[beam_iter & 1u], ((beam_iter >> 1) & 1u) ^ 1u, abort_flag) && ok;
           tc_fence_after();
           if (ok) {
             const uint32_t base = op_addr + st * stage_bytes;
+            if (DO_CORR) {
 #pragma unroll
-            for (int ks = 0; ks < KBLK / 16; ++ks) {
-              const uint32_t acc = (!chunk_start || ks > 0) ? 1u : 0u;
-              umma_f16(tmem, umma_desc_sw128(base + ks * 32), umma_desc_sw128(base + ks * 32),
-                       idesc_main, acc);
-              if (corner)
-                umma_f16(tmem + NR, umma_desc_sw128(base + (NR - 128) * 128 + ks * 32),
-                         umma_desc_sw128(base + 128 * 128 + ks * 32), idesc_corner, acc);
+              for (int ks = 0; ks < KBLK / 16; ++ks) {
+                const uint32_t acc = (!chunk_start || ks > 0) ? 1u : 0u;
+                umma_f16(tmem, umma_desc_sw128(base + ks * 32), umma_desc_sw128(base + ks * 32),
+                         idesc_main, acc);
+                if (corner)
+                  umma_f16(tmem + NR, umma_desc_sw128(base + (NR - 128) * 128 + ks * 32),
+                           umma_desc_sw128(base + 128 * 128 + ks * 32), idesc_corner, acc);
+              }
+            }
+            if (beam_now) {
+              // the pair (st - 1, st): samples 0..63 and 64..127 of this tile
+              const uint32_t abase = base - stage_bytes;
+              const uint32_t wbase = w_addr + wb * a.wtile_bytes;
+              const uint32_t d = tmem + a.beam_off + (beam_iter & 1u) * a.BN;
+              for (int ks = 0; ks < NR / 16; ++ks) {
+                const uint64_t ad = desc_sw128(abase + ks * 16 * 128, stage_bytes, 1024);
+                const uint32_t kcol = ks * 16;
+                const uint64_t bd =
+                    desc_sw128(wbase + (kcol / 64) * (a.BN * 128) + (kcol % 64) * 2, 16, 1024);
+                umma_f16(d, ad, bd, idesc_beam, ks > 0 ? 1u : 0u);
+              }
             }
           } else {
             failed = true;
           }
-          umma_commit(&h.op_empty[st]);
-          if ((kb % CHUNK_KBLK) == CHUNK_KBLK - 1 || kb == a.nkb - 1) {
+          if (!DO_BEAM) {
+            umma_commit(&h.op_empty[st]);
+          } else if (kb & 1) {
+            umma_commit(&h.op_empty[(st + NUM_OP_STAGES - 1) % NUM_OP_STAGES]);
+            umma_commit(&h.op_empty[st]);
+            umma_commit(&h.beam_full[beam_iter & 1u]);
+            ++beam_iter;
+          }
+          if (DO_CORR && ((kb % CHUNK_KBLK) == CHUNK_KBLK - 1 || kb == a.nkb - 1)) {
             umma_commit(&h.acc_full);
             ++acc_iter;
           }
           ++op_iter;
         }
+        if (DO_BEAM) umma_commit(&h.w_empty[wb]);
       }
       umma_commit(&h.mma_done);
       mbar_wait_drain(&h.mma_done, 0);
@@ -259,11 +328,40 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
     const int NR = a.NR;
     const int ncols = NR + (NR > 128 ? NR - 128 : 0);
     const int R4 = 4 * R;
-    uint32_t acc_iter = 0;
+    uint32_t acc_iter = 0, beam_iter = 0;
     bool failed = false;
     for (int c = blockIdx.x; c < a.C; c += gridDim.x) {
-      for (int ch = 0; ch < nchunks; ++ch) {
-        const bool ok = mbar_wait(&h.acc_full, acc_iter & 1u, abort_flag);
+      for (int kb = 0; kb < a.nkb; ++kb) {
+        if (DO_BEAM && (kb & 1)) {
+          const uint32_t buf = beam_iter & 1u;
+          const bool ok = mbar_wait(&h.beam_full[buf], (beam_iter >> 1) & 1u, abort_flag, 32);
+          failed |= !ok;
+          tc_fence_after();
+          const int t = (kb >> 1) * 128 + ew * 32 + lane;
+          for (int cb = 0; cb < a.BN / 16; ++cb) {
+            uint32_t v[16];
+            tmem_ld16(tmem + a.beam_off + buf * a.BN + cb * 16, v);
+            tmem_wait_ld();
+            if (ok && t < T) {
+#pragma unroll
+              for (int e2 = 0; e2 < 8; ++e2) {
+                const int col = cb * 8 + e2;  // complex column (pol, beam)
+                const int p = col / a.NB;
+                const int m = col - p * a.NB;
+                if (p < 2)
+                  a.beams[(((size_t)c * 2 + p) * a.NB + m) * T + t] =
+                      __floats2half2_rn(__uint_as_float(v[2 * e2]), __uint_as_float(v[2 * e2 + 1]));
+              }
+            }
+          }
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&h.beam_empty[buf]);
+          ++beam_iter;
+        }
+        if (!DO_CORR || !((kb % CHUNK_KBLK) == CHUNK_KBLK - 1 || kb == a.nkb - 1)) continue;
+        const int ch = kb / CHUNK_KBLK;
+        const bool ok = mbar_wait(&h.acc_full, acc_iter & 1u, abort_flag, 32);
         failed |= !ok;
         tc_fence_after();
         const bool first = ch == 0;
@@ -271,7 +369,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
         for (int cb = 0; cb < ncols / 16; ++cb) {
           uint32_t fv[16], sv[16];
           tmem_ld16(tmem + cb * 16, fv);
-          if (!first) tmem_ld16(tmem + TMEM_I32 + cb * 16, sv);
+          if (!first) tmem_ld16(tmem + a.i32_off + cb * 16, sv);
           tmem_wait_ld();
           int acc[16];
 #pragma unroll
@@ -281,7 +379,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
             uint32_t out[16];
 #pragma unroll
             for (int e = 0; e < 16; ++e) out[e] = static_cast<uint32_t>(acc[e]);
-            tmem_st16(tmem + TMEM_I32 + cb * 16, out);
+            tmem_st16(tmem + a.i32_off + cb * 16, out);
             continue;
           }
           // Final chunk of this channel: combine (re, im) row pairs and write.
@@ -320,16 +418,59 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
   } else if (warp >= WARP_CONV0 || warp == 2 || warp == 3) {
     // ---------------- converters ----------------
     const int ct = warp >= WARP_CONV0 ? (warp - WARP_CONV0 + 2) * 32 + lane : (warp - 2) * 32 + lane;
-    uint32_t g_base = 0, op_iter = 0;
+    uint32_t g_base = 0, op_iter = 0, cw = 0;
     bool failed = false;
     const int Rpp4 = a.Rpp * 4;
-    for (int c = blockIdx.x; c < a.C; c += gridDim.x) {
+    for (int c = blockIdx.x; c < a.C; c += gridDim.x, ++cw) {
+      if (DO_BEAM) {
+        // weight tile for this channel: B[n][u], n = (pol, beam, re/im), K-major,
+        // 128-byte swizzle, one [BN rows][64 cols] block per K atom
+        const uint32_t wb = cw & 1u;
+        const bool ok = mbar_wait(&h.w_empty[wb], ((cw >> 1) & 1u) ^ 1u, abort_flag);
+        failed |= !ok;
+        if (ok) {
+          uint8_t *wt = w_ptr + wb * a.wtile_bytes;
+          const int nchunk = a.katoms * 8;  // 16-byte chunks per row
+          for (int task = ct; task < a.BN * nchunk; task += NUM_CONV_THREADS) {
+            const int n = task / nchunk;
+            const int ch = task - n * nchunk;
+            const int atom = ch >> 3, cc = ch & 7;
+            const int pn = n / (2 * a.NB);
+            const int mn = (n >> 1) - pn * a.NB;
+            const int cn = n & 1;
+            uint32_t pk[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              float vals[2];
+#pragma unroll
+              for (int dd = 0; dd < 2; ++dd) {
+                const int u = atom * 64 + cc * 8 + q * 2 + dd;
+                float v = 0.0f;
+                const int ku = u >> 1, cu = u & 1;
+                if (pn < 2 && u < 4 * R && ku / R == pn) {
+                  const int r = ku - pn * R;
+                  const float2 w = a.weff[(((size_t)c * 2 + pn) * a.NBW + mn) * R + r];
+                  v = cn == 0 ? (cu == 0 ? w.x : -w.y) : (cu == 0 ? w.y : w.x);
+                }
+                vals[dd] = v;
+              }
+              pk[q] = u32_of(__floats2half2_rn(vals[0], vals[1]));
+            }
+            *reinterpret_cast<uint4 *>(wt + atom * (a.BN * 128) + n * 128 + ((cc ^ (n & 7)) << 4)) =
+                make_uint4(pk[0], pk[1], pk[2], pk[3]);
+          }
+        }
+        fence_proxy_async_smem();
+        named_bar_sync(1, NUM_CONV_THREADS);
+        if (ct == 0) mbar_arrive(&h.w_full[wb]);
+      }
       int q_rel = qa0;
       for (int kb = 0; kb < a.nkb; ++kb) {
         const int s0 = kb * KBLK;
         const int s1 = min(s0 + KBLK - 1, T - 1);
-        const int qa = (s0 + off_min) / Tp;
-        const int qb = min(a.P + 1, (s1 + off_max) / Tp);
+        const bool live = s0 < T;  // a beam pair's padding block holds no samples
+        const int qa = live ? (s0 + off_min) / Tp : qbN + 1;
+        const int qb = live ? min(a.P + 1, (s1 + off_max) / Tp) : qbN;
         bool ok = true;
         for (int q = qa; q <= qb && ok; ++q) {
           const uint32_t gq = g_base + (q - qa0);
@@ -346,37 +487,35 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
             const int f = r / a.Rpp;
             const int n = r - f * a.Rpp;
             const int sfirst = s0 + oct * 8;
-            // packet / time of the first sample, then step forward
-            int qq = sfirst + h.offsets[f];
-            int pkt = qq / Tp;
-            int tt = qq - pkt * Tp;
-            const uint8_t *slot_ptr = ring_ptr + (size_t)((g_base + (pkt - qa0)) & ns_mask) * a.slot_stride;
-            uint32_t scw = *reinterpret_cast<const uint32_t *>(slot_ptr + a.slot_bytes + r * 4);
-            const uint8_t *src = slot_ptr + (f * Tp + tt) * Rpp4 + n * 4;
+            uint32_t word[8], scw[8];
+            {
+              // addresses of the 8 samples (at most a few packet crossings)
+              const int qq = sfirst + h.offsets[f];
+              int pkt = qq / Tp;
+              int tt = qq - pkt * Tp;
+#pragma unroll
+              for (int e = 0; e < 8; ++e) {
+                if (sfirst + e < T) {
+                  const uint8_t *slot_ptr =
+                      ring_ptr + (size_t)((g_base + (pkt - qa0)) & ns_mask) * a.slot_stride;
+                  word[e] = *reinterpret_cast<const uint32_t *>(slot_ptr + (f * Tp + tt) * Rpp4 + n * 4);
+                  scw[e] = *reinterpret_cast<const uint32_t *>(slot_ptr + a.slot_bytes + r * 4);
+                } else {
+                  word[e] = 0;
+                  scw[e] = 0;
+                }
+                if (++tt == Tp) {
+                  tt = 0;
+                  ++pkt;
+                }
+              }
+            }
             uint32_t col[4][4];  // [row: p0re, p0im, p1re, p1im][pair of samples]
 #pragma unroll
             for (int e = 0; e < 8; e += 2) {
               __half2 v0[2], v1[2];
-#pragma unroll
-              for (int dd = 0; dd < 2; ++dd) {
-                uint32_t word = 0, sc = 0;
-                if (sfirst + e + dd < T) {
-                  word = *reinterpret_cast<const uint32_t *>(src);
-                  sc = scw;
-                }
-                convert_word(word, sc, v0[dd], v1[dd]);
-                // advance one sample (crossing into the next packet's slot if needed)
-                if (++tt == Tp) {
-                  tt = 0;
-                  ++pkt;
-                  slot_ptr = ring_ptr + (size_t)((g_base + (pkt - qa0)) & ns_mask) * a.slot_stride;
-                  if (sfirst + e + dd + 1 < T)
-                    scw = *reinterpret_cast<const uint32_t *>(slot_ptr + a.slot_bytes + r * 4);
-                  src = slot_ptr + (f * Tp) * Rpp4 + n * 4;
-                } else {
-                  src += Rpp4;
-                }
-              }
+              convert_word(word[e], scw[e], v0[0], v1[0]);
+              convert_word(word[e + 1], scw[e + 1], v0[1], v1[1]);
               col[0][e >> 1] = __byte_perm(u32_of(v0[0]), u32_of(v0[1]), 0x5410);
               col[1][e >> 1] = __byte_perm(u32_of(v0[0]), u32_of(v0[1]), 0x7632);
               col[2][e >> 1] = __byte_perm(u32_of(v1[0]), u32_of(v1[1]), 0x5410);
@@ -396,7 +535,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
         named_bar_sync(1, NUM_CONV_THREADS);
         if (ct == 0) {
           mbar_arrive(&h.op_full[st]);
-          const int next = (kb + 1 < a.nkb) ? ((kb + 1) * KBLK + off_min) / Tp : qbN + 1;
+          int next = qbN + 1;
+          if (kb + 1 < a.nkb && (kb + 1) * KBLK < T) next = ((kb + 1) * KBLK + off_min) / Tp;
           for (; q_rel < next; ++q_rel) {
             const uint32_t gq = g_base + (q_rel - qa0);
             mbar_arrive(&h.pk_empty[gq & ns_mask]);
@@ -413,12 +553,31 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corr_kernel(const CorrArgs a) 
   __syncthreads();
   if (warp == WARP_MMA) {
     tc_fence_after();
-    tmem_dealloc(h.tmem_base, TMEM_COLS);
+    tmem_dealloc(h.tmem_base, a.tmem_cols);
   }
 }
 
 int g_max_smem = 0;
-int g_attr_set = 0;
+bool g_attr_set[4] = {false, false, false, false};
+
+template <bool DO_CORR, bool DO_BEAM>
+cudaError_t launch_mode(const CorrArgs &a, size_t smem, int grid, cudaStream_t stream) {
+  const int idx = (DO_CORR ? 1 : 0) + (DO_BEAM ? 2 : 0);
+  if (!g_attr_set[idx]) {
+    cudaError_t e = cudaFuncSetAttribute(sf_corrbeam_kernel<DO_CORR, DO_BEAM>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem);
+    if (e != cudaSuccess) return e;
+    g_attr_set[idx] = true;
+  }
+  sf_corrbeam_kernel<DO_CORR, DO_BEAM><<<grid, NTHREADS, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
+uint32_t pow2_at_least(uint32_t x) {
+  uint32_t p = 32;
+  while (p < x) p <<= 1;
+  return p;
+}
 
 }  // namespace
 
@@ -433,13 +592,23 @@ int sf_correlate_supported(const sf_plan *p, char *why, size_t why_len) {
   return 1;
 }
 
-cudaError_t sf_launch_correlate(const sf_plan *p, const int8_t *samples, const int16_t *scales,
-                                const int32_t *offsets, int32_t *vis, cudaStream_t stream) {
+int sf_beam_tc_supported(const sf_plan *p, int n_beams_out) {
+  return p->R <= MAX_R && p->F <= MAX_F && (p->R * p->Tp * 4) % 16 == 0 && n_beams_out <= MAX_BEAM_OUT;
+}
+
+// mode bit 0: correlate, bit 1: beamform (n_beams_out beams per pol from the
+// plan's effective weights).
+cudaError_t sf_launch_corrbeam(const sf_plan *p, const int8_t *samples, const int16_t *scales,
+                               const int32_t *offsets, int32_t *vis, int n_beams_out, __half2 *beams,
+                               int mode, cudaStream_t stream) {
+  const bool do_corr = mode & 1, do_beam = (mode & 2) != 0;
   CorrArgs a;
   a.samples = samples;
   a.scales = scales;
   a.offsets = offsets;
   a.vis = vis;
+  a.weff = p->d_weff;
+  a.beams = beams;
   a.status = p->d_status;
   a.C = p->C;
   a.F = p->F;
@@ -452,15 +621,36 @@ cudaError_t sf_launch_correlate(const sf_plan *p, const int8_t *samples, const i
   a.NR = ((4 * p->R + 15) / 16) * 16;
   a.stage_rows = std::max(a.NR, 128);
   a.nkb = (p->T + KBLK - 1) / KBLK;
+  if (do_beam) a.nkb = (a.nkb + 1) & ~1;
   a.slot_bytes = p->R * p->Tp * 4;
   a.slot_stride = a.slot_bytes + ((p->R * 4 + 15) / 16) * 16;
+  a.NB = n_beams_out;
+  a.NBW = 2 * p->B;
+  a.BN = ((4 * n_beams_out + 15) / 16) * 16;
+  a.katoms = (a.NR + 63) / 64;
+  a.wtile_bytes = do_beam ? static_cast<uint32_t>(a.katoms * a.BN * 128) : 0u;
+  const int ncols = a.NR + (a.NR > 128 ? a.NR - 128 : 0);
+  if (do_corr && do_beam) {
+    a.beam_off = ncols;
+    a.i32_off = ncols + 2 * a.BN;
+    a.tmem_cols = pow2_at_least(a.i32_off + ncols);
+  } else if (do_corr) {
+    a.beam_off = 0;
+    a.i32_off = 256;
+    a.tmem_cols = 512;
+  } else {
+    a.beam_off = 0;
+    a.i32_off = 0;
+    a.tmem_cols = pow2_at_least(2 * a.BN);
+  }
+  if (a.tmem_cols > 512) return cudaErrorInvalidConfiguration;
 
   if (!g_max_smem) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&g_max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   }
-  const size_t fixed = HEADER_BYTES + 1024 + (size_t)NUM_OP_STAGES * a.stage_rows * 128;
+  const size_t fixed = HEADER_BYTES + 1024 + (size_t)NUM_OP_STAGES * a.stage_rows * 128 + 2 * a.wtile_bytes;
   const int need_slots = 63 / p->Tp + 5;
   long avail = (long)g_max_smem - (long)fixed;
   int ns = avail > 0 ? (int)std::min<long>(MAX_SLOTS, avail / a.slot_stride) : 0;
@@ -468,13 +658,13 @@ cudaError_t sf_launch_correlate(const sf_plan *p, const int8_t *samples, const i
   if (ns < need_slots) return cudaErrorInvalidConfiguration;
   a.num_slots = ns;
   const size_t smem = fixed + (size_t)ns * a.slot_stride;
-  if (!g_attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(sf_corr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         g_max_smem);
-    if (e != cudaSuccess) return e;
-    g_attr_set = 1;
-  }
   const int grid = std::max(1, std::min(p->C, p->num_sms));
-  sf_corr_kernel<<<grid, NTHREADS, smem, stream>>>(a);
-  return cudaGetLastError();
+  if (do_corr && do_beam) return launch_mode<true, true>(a, smem, grid, stream);
+  if (do_corr) return launch_mode<true, false>(a, smem, grid, stream);
+  return launch_mode<false, true>(a, smem, grid, stream);
+}
+
+cudaError_t sf_launch_correlate(const sf_plan *p, const int8_t *samples, const int16_t *scales,
+                                const int32_t *offsets, int32_t *vis, cudaStream_t stream) {
+  return sf_launch_corrbeam(p, samples, scales, offsets, vis, 0, nullptr, 1, stream);
 }

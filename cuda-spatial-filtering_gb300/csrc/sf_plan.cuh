@@ -40,6 +40,11 @@ struct sf_plan {
 cudaError_t sf_launch_correlate(const sf_plan *p, const int8_t *samples, const int16_t *scales,
                                 const int32_t *offsets, int32_t *vis, cudaStream_t stream);
 int sf_correlate_supported(const sf_plan *p, char *why, size_t why_len);
+// Tensor-core correlate (mode bit 0) and/or beamform (bit 1) in one pass.
+cudaError_t sf_launch_corrbeam(const sf_plan *p, const int8_t *samples, const int16_t *scales,
+                               const int32_t *offsets, int32_t *vis, int n_beams_out, __half2 *beams,
+                               int mode, cudaStream_t stream);
+int sf_beam_tc_supported(const sf_plan *p, int n_beams_out);
 
 cudaError_t sf_launch_eig(const sf_plan *p, const int32_t *vis, int eig_mode, int k_rule,
                           float delta, int shrink, float *evals, float2 *evecs, int32_t *counts,
