@@ -78,6 +78,8 @@ struct CorrArgs {
   int katoms;       // 64-column K atoms of the weight tile: ceil(NR / 64)
   uint32_t wtile_bytes;
   uint32_t tmem_cols, i32_off, beam_off;
+  int nacc;  // fp32 chunk accumulators in tensor memory (2 = double-buffered)
+  uint32_t acc_stride;  // tensor-memory columns between the fp32 accumulators
 };
 
 struct __align__(8) Header {
@@ -85,8 +87,8 @@ struct __align__(8) Header {
   uint64_t pk_empty[MAX_SLOTS];
   uint64_t op_full[NUM_OP_STAGES];
   uint64_t op_empty[NUM_OP_STAGES];
-  uint64_t acc_full;
-  uint64_t acc_empty;
+  uint64_t acc_full[2];
+  uint64_t acc_empty[2];
   uint64_t beam_full[2];
   uint64_t beam_empty[2];
   uint64_t w_full[2];
@@ -176,8 +178,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
       mbar_init(&h.op_full[s], 1);
       mbar_init(&h.op_empty[s], 1);
     }
-    mbar_init(&h.acc_full, 1);
-    mbar_init(&h.acc_empty, 4);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&h.acc_full[b], 1);
+      mbar_init(&h.acc_empty[b], 4);
+    }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&h.beam_full[b], 1);
       mbar_init(&h.beam_empty[b], 4);
@@ -255,7 +259,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
       const int NR = a.NR;
       const bool corner = NR > 128;
       const uint32_t idesc_main = umma_idesc_f16_f32(128, NR);
-      const uint32_t idesc_corner = umma_idesc_f16_f32(128, corner ? NR - 128 : 16);
+      // rows 128..NR-1 come from an M=64 MMA over rows NR-64..NR-1 (its
+      // accumulator rows l sit in lanes (l % 16) + 32 (l / 16))
+      const uint32_t idesc_corner = umma_idesc_f16_f32(64, corner ? NR - 128 : 16);
       // beam: A (samples) MN-major, B (weights) K-major, M = 128 samples, N = BN
       const uint32_t idesc_beam = umma_idesc_f16_f32(128, a.BN) | (1u << 15);
       uint32_t op_iter = 0, acc_iter = 0, beam_iter = 0, cw = 0;
@@ -267,7 +273,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
           const uint32_t st = op_iter % NUM_OP_STAGES;
           bool ok = mbar_wait(&h.op_full[st], (op_iter / NUM_OP_STAGES) & 1u, abort_flag);
           const bool chunk_start = (kb % CHUNK_KBLK) == 0;
-          if (DO_CORR && chunk_start) ok = mbar_wait(&h.acc_empty, (acc_iter & 1u) ^ 1u, abort_flag) && ok;
+          const uint32_t abuf = acc_iter % a.nacc;
+          if (DO_CORR && chunk_start)
+            ok = mbar_wait(&h.acc_empty[abuf], ((acc_iter / a.nacc) & 1u) ^ 1u, abort_flag) && ok;
           const bool beam_now = DO_BEAM && (kb & 1);
           if (beam_now)
             ok = mbar_wait(&h.beam_empty[beam_iter & 1u], ((beam_iter >> 1) & 1u) ^ 1u, abort_flag) && ok;
@@ -275,13 +283,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
           if (ok) {
             const uint32_t base = op_addr + st * stage_bytes;
             if (DO_CORR) {
+              const uint32_t dacc = tmem + abuf * a.acc_stride;
 #pragma unroll
               for (int ks = 0; ks < KBLK / 16; ++ks) {
                 const uint32_t acc = (!chunk_start || ks > 0) ? 1u : 0u;
-                umma_f16(tmem, umma_desc_sw128(base + ks * 32), umma_desc_sw128(base + ks * 32),
+                umma_f16(dacc, umma_desc_sw128(base + ks * 32), umma_desc_sw128(base + ks * 32),
                          idesc_main, acc);
                 if (corner)
-                  umma_f16(tmem + NR, umma_desc_sw128(base + (NR - 128) * 128 + ks * 32),
+                  umma_f16(dacc + NR, umma_desc_sw128(base + (NR - 64) * 128 + ks * 32),
                            umma_desc_sw128(base + 128 * 128 + ks * 32), idesc_corner, acc);
               }
             }
@@ -310,7 +319,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
             ++beam_iter;
           }
           if (DO_CORR && ((kb % CHUNK_KBLK) == CHUNK_KBLK - 1 || kb == a.nkb - 1)) {
-            umma_commit(&h.acc_full);
+            umma_commit(&h.acc_full[abuf]);
             ++acc_iter;
           }
           ++op_iter;
@@ -361,14 +370,16 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
         }
         if (!DO_CORR || !((kb % CHUNK_KBLK) == CHUNK_KBLK - 1 || kb == a.nkb - 1)) continue;
         const int ch = kb / CHUNK_KBLK;
-        const bool ok = mbar_wait(&h.acc_full, acc_iter & 1u, abort_flag, 32);
+        const uint32_t abuf = acc_iter % a.nacc;
+        const bool ok = mbar_wait(&h.acc_full[abuf], (acc_iter / a.nacc) & 1u, abort_flag, 32);
         failed |= !ok;
         tc_fence_after();
         const bool first = ch == 0;
         const bool last = ch == nchunks - 1;
+        const uint32_t tacc = tmem + abuf * a.acc_stride;
         for (int cb = 0; cb < ncols / 16; ++cb) {
           uint32_t fv[16], sv[16];
-          tmem_ld16(tmem + cb * 16, fv);
+          tmem_ld16(tacc + cb * 16, fv);
           if (!first) tmem_ld16(tmem + a.i32_off + cb * 16, sv);
           tmem_wait_ld();
           int acc[16];
@@ -384,7 +395,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
           }
           // Final chunk of this channel: combine (re, im) row pairs and write.
           const bool main_region = cb * 16 < NR;
-          const int u = main_region ? ew * 32 + lane : (NR - 128) + ew * 32 + lane;
+          const int u = main_region ? ew * 32 + lane : (lane < 16 ? (NR - 64) + ew * 16 + lane : 1 << 20);
           const int k = u >> 1;
           const int comp = u & 1;
           const int p = k / R;
@@ -410,7 +421,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
         if (!last) tmem_wait_st();
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&h.acc_empty);
+        if (lane == 0) mbar_arrive(&h.acc_empty[abuf]);
         ++acc_iter;
       }
     }
@@ -464,85 +475,127 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
         named_bar_sync(1, NUM_CONV_THREADS);
         if (ct == 0) mbar_arrive(&h.w_full[wb]);
       }
-      int q_rel = qa0;
-      for (int kb = 0; kb < a.nkb; ++kb) {
+      int q_rel = qa0;   // next packet to release
+      int q_wait = qa0;  // next packet not yet waited for
+      // per-task packet/time cursor of the task's first sample, advanced by
+      // one K block (64 samples) at a time: no division in the loop
+      int cur_pkt[2], cur_tt[2];
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int task = ct + j * NUM_CONV_THREADS;
+        const int r = (task >> 3) < R ? (task >> 3) : 0;
+        const int qq = (task & 7) * 8 + h.offsets[r / a.Rpp];
+        cur_pkt[j] = qq / Tp;
+        cur_tt[j] = qq - cur_pkt[j] * Tp;
+      }
+      for (int kb = 0; kb < a.nkb; kb += 2) {
         const int s0 = kb * KBLK;
-        const int s1 = min(s0 + KBLK - 1, T - 1);
-        const bool live = s0 < T;  // a beam pair's padding block holds no samples
-        const int qa = live ? (s0 + off_min) / Tp : qbN + 1;
-        const int qb = live ? min(a.P + 1, (s1 + off_max) / Tp) : qbN;
+        const int qb = s0 < T ? min(a.P + 1, (min(s0 + 2 * KBLK - 1, T - 1) + off_max) / Tp) : qbN;
         bool ok = true;
-        for (int q = qa; q <= qb && ok; ++q) {
-          const uint32_t gq = g_base + (q - qa0);
+        for (; q_wait <= qb && ok; ++q_wait) {
+          const uint32_t gq = g_base + (q_wait - qa0);
           ok = mbar_wait(&h.pk_full[gq & ns_mask], (gq >> ns_shift) & 1u, abort_flag);
         }
-        const uint32_t st = op_iter % NUM_OP_STAGES;
-        ok = ok && mbar_wait(&h.op_empty[st], ((op_iter / NUM_OP_STAGES) & 1u) ^ 1u, abort_flag);
+        const uint32_t st0 = op_iter % NUM_OP_STAGES;
+        const uint32_t st1 = (op_iter + 1) % NUM_OP_STAGES;
+        ok = ok && mbar_wait(&h.op_empty[st0], ((op_iter / NUM_OP_STAGES) & 1u) ^ 1u, abort_flag);
+        ok = ok && mbar_wait(&h.op_empty[st1], (((op_iter + 1) / NUM_OP_STAGES) & 1u) ^ 1u, abort_flag);
         failed |= !ok;
-        if (ok) {
-          uint8_t *stage = op_ptr + st * stage_bytes;
-          for (int task = ct; task < R * 8; task += NUM_CONV_THREADS) {
+        const bool fast = (s0 + 2 * KBLK <= T) && Tp >= 8;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          const int task = ct + j * NUM_CONV_THREADS;
+          if (ok && task < R * 8) {
             const int oct = task & 7;
             const int r = task >> 3;
             const int f = r / a.Rpp;
             const int n = r - f * a.Rpp;
-            const int sfirst = s0 + oct * 8;
-            uint32_t word[8], scw[8];
-            {
-              // addresses of the 8 samples (at most a few packet crossings)
-              const int qq = sfirst + h.offsets[f];
-              int pkt = qq / Tp;
-              int tt = qq - pkt * Tp;
+            const uint32_t fn_off = static_cast<uint32_t>((f * Tp) * Rpp4 + n * 4);
+            uint32_t word[2][8], scw[2][8];
 #pragma unroll
-              for (int e = 0; e < 8; ++e) {
-                if (sfirst + e < T) {
-                  const uint8_t *slot_ptr =
-                      ring_ptr + (size_t)((g_base + (pkt - qa0)) & ns_mask) * a.slot_stride;
-                  word[e] = *reinterpret_cast<const uint32_t *>(slot_ptr + (f * Tp + tt) * Rpp4 + n * 4);
-                  scw[e] = *reinterpret_cast<const uint32_t *>(slot_ptr + a.slot_bytes + r * 4);
-                } else {
-                  word[e] = 0;
-                  scw[e] = 0;
+            for (int b = 0; b < 2; ++b) {
+              // cursor of this block's first sample
+              int pkt = cur_pkt[j], tt = cur_tt[j];
+              if (b) {
+                tt += KBLK;
+                while (tt >= Tp) { tt -= Tp; ++pkt; }
+              }
+              if (fast) {
+                const uint8_t *slot_a = ring_ptr + (size_t)((g_base + (pkt - qa0)) & ns_mask) * a.slot_stride;
+                const uint8_t *slot_b = ring_ptr + (size_t)((g_base + (pkt + 1 - qa0)) & ns_mask) * a.slot_stride;
+                const uint32_t sc_a = *reinterpret_cast<const uint32_t *>(slot_a + a.slot_bytes + r * 4);
+                const uint32_t sc_b = tt + 7 >= Tp
+                                          ? *reinterpret_cast<const uint32_t *>(slot_b + a.slot_bytes + r * 4)
+                                          : sc_a;
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                  const int t = tt + e;
+                  const bool cross = t >= Tp;
+                  const uint8_t *sp = cross ? slot_b : slot_a;
+                  word[b][e] = *reinterpret_cast<const uint32_t *>(sp + fn_off + (cross ? t - Tp : t) * Rpp4);
+                  scw[b][e] = cross ? sc_b : sc_a;
                 }
-                if (++tt == Tp) {
-                  tt = 0;
-                  ++pkt;
+              } else {
+                const int sfirst = s0 + b * KBLK + oct * 8;
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                  if (sfirst + e < T) {
+                    const uint8_t *slot_ptr = ring_ptr + (size_t)((g_base + (pkt - qa0)) & ns_mask) * a.slot_stride;
+                    word[b][e] = *reinterpret_cast<const uint32_t *>(slot_ptr + fn_off + tt * Rpp4);
+                    scw[b][e] = *reinterpret_cast<const uint32_t *>(slot_ptr + a.slot_bytes + r * 4);
+                  } else {
+                    word[b][e] = 0;
+                    scw[b][e] = 0;
+                  }
+                  if (++tt == Tp) {
+                    tt = 0;
+                    ++pkt;
+                  }
                 }
               }
             }
-            uint32_t col[4][4];  // [row: p0re, p0im, p1re, p1im][pair of samples]
 #pragma unroll
-            for (int e = 0; e < 8; e += 2) {
-              __half2 v0[2], v1[2];
-              convert_word(word[e], scw[e], v0[0], v1[0]);
-              convert_word(word[e + 1], scw[e + 1], v0[1], v1[1]);
-              col[0][e >> 1] = __byte_perm(u32_of(v0[0]), u32_of(v0[1]), 0x5410);
-              col[1][e >> 1] = __byte_perm(u32_of(v0[0]), u32_of(v0[1]), 0x7632);
-              col[2][e >> 1] = __byte_perm(u32_of(v1[0]), u32_of(v1[1]), 0x5410);
-              col[3][e >> 1] = __byte_perm(u32_of(v1[0]), u32_of(v1[1]), 0x7632);
-            }
+            for (int b = 0; b < 2; ++b) {
+              uint32_t col[4][4];  // [row: p0re, p0im, p1re, p1im][pair of samples]
 #pragma unroll
-            for (int rr = 0; rr < 4; ++rr) {
-              const int pol = rr >> 1;
-              const int comp = rr & 1;
-              const int u = 2 * (pol * R + r) + comp;
-              uint4 *dst = reinterpret_cast<uint4 *>(stage + u * 128 + ((oct ^ (u & 7)) << 4));
-              *dst = make_uint4(col[rr][0], col[rr][1], col[rr][2], col[rr][3]);
+              for (int e = 0; e < 8; e += 2) {
+                __half2 v0[2], v1[2];
+                convert_word(word[b][e], scw[b][e], v0[0], v1[0]);
+                convert_word(word[b][e + 1], scw[b][e + 1], v0[1], v1[1]);
+                col[0][e >> 1] = __byte_perm(u32_of(v0[0]), u32_of(v0[1]), 0x5410);
+                col[1][e >> 1] = __byte_perm(u32_of(v0[0]), u32_of(v0[1]), 0x7632);
+                col[2][e >> 1] = __byte_perm(u32_of(v1[0]), u32_of(v1[1]), 0x5410);
+                col[3][e >> 1] = __byte_perm(u32_of(v1[0]), u32_of(v1[1]), 0x7632);
+              }
+              uint8_t *stage = op_ptr + (b ? st1 : st0) * stage_bytes;
+#pragma unroll
+              for (int rr = 0; rr < 4; ++rr) {
+                const int pol = rr >> 1;
+                const int comp = rr & 1;
+                const int u = 2 * (pol * R + r) + comp;
+                uint4 *dst = reinterpret_cast<uint4 *>(stage + u * 128 + ((oct ^ (u & 7)) << 4));
+                *dst = make_uint4(col[rr][0], col[rr][1], col[rr][2], col[rr][3]);
+              }
             }
           }
+          // advance the cursor by two K blocks
+          cur_tt[j] += 2 * KBLK;
+          while (cur_tt[j] >= Tp) { cur_tt[j] -= Tp; ++cur_pkt[j]; }
         }
         fence_proxy_async_smem();
         named_bar_sync(1, NUM_CONV_THREADS);
-        if (ct == 0) {
-          mbar_arrive(&h.op_full[st]);
+        // bookkeeping on the last converter thread
+        if (ct == NUM_CONV_THREADS - 1) {
+          mbar_arrive(&h.op_full[st0]);
+          mbar_arrive(&h.op_full[st1]);
           int next = qbN + 1;
-          if (kb + 1 < a.nkb && (kb + 1) * KBLK < T) next = ((kb + 1) * KBLK + off_min) / Tp;
+          if (kb + 2 < a.nkb && (kb + 2) * KBLK < T) next = ((kb + 2) * KBLK + off_min) / Tp;
           for (; q_rel < next; ++q_rel) {
             const uint32_t gq = g_base + (q_rel - qa0);
             mbar_arrive(&h.pk_empty[gq & ns_mask]);
           }
         }
-        ++op_iter;
+        op_iter += 2;
       }
       g_base += npk;
     }
@@ -620,8 +673,7 @@ cudaError_t sf_launch_corrbeam(const sf_plan *p, const int8_t *samples, const in
   a.NBL = p->NBL;
   a.NR = ((4 * p->R + 15) / 16) * 16;
   a.stage_rows = std::max(a.NR, 128);
-  a.nkb = (p->T + KBLK - 1) / KBLK;
-  if (do_beam) a.nkb = (a.nkb + 1) & ~1;
+  a.nkb = ((p->T + KBLK - 1) / KBLK + 1) & ~1;  // converters fill K blocks in pairs
   a.slot_bytes = p->R * p->Tp * 4;
   a.slot_stride = a.slot_bytes + ((p->R * 4 + 15) / 16) * 16;
   a.NB = n_beams_out;
@@ -630,13 +682,20 @@ cudaError_t sf_launch_corrbeam(const sf_plan *p, const int8_t *samples, const in
   a.katoms = (a.NR + 63) / 64;
   a.wtile_bytes = do_beam ? static_cast<uint32_t>(a.katoms * a.BN * 128) : 0u;
   const int ncols = a.NR + (a.NR > 128 ? a.NR - 128 : 0);
+  a.nacc = 1;
+  a.acc_stride = ncols;
   if (do_corr && do_beam) {
     a.beam_off = ncols;
     a.i32_off = ncols + 2 * a.BN;
     a.tmem_cols = pow2_at_least(a.i32_off + ncols);
   } else if (do_corr) {
     a.beam_off = 0;
-    a.i32_off = 256;
+    if (3 * ncols <= 512) {
+      a.nacc = 2;  // drain one chunk while the next accumulates
+      a.i32_off = 2 * ncols;
+    } else {
+      a.i32_off = 256;
+    }
     a.tmem_cols = 512;
   } else {
     a.beam_off = 0;
