@@ -65,18 +65,31 @@ SF_DEVICE bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
+// try_wait that may suspend the thread for up to `hint_ns` nanoseconds; the
+// thread resumes as soon as the phase completes.
+SF_DEVICE bool mbar_try_wait_suspend(uint64_t *bar, uint32_t parity, uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+
 // Wait for the phase with the given parity to complete.  Returns false (and
 // raises *abort) when SF_WAIT_CYCLES clock cycles pass or another role has
 // already aborted, so no thread of the CTA can spin forever.  Roles that wait
-// long (producer, epilogue) pass a sleep between polls so their spinning does
-// not take issue slots from the converter warps.
-SF_DEVICE bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort, uint32_t sleep_ns = 0) {
+// long (producer, epilogue) pass a suspend hint so the hardware parks them
+// until the phase completes instead of spinning on issue slots.
+SF_DEVICE bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort, uint32_t suspend_ns = 0) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   uint32_t n = 0;
-  while (!mbar_try_wait(bar, parity)) {
-    if (sleep_ns) __nanosleep(sleep_ns);
-    if ((++n & 63u) == 0) {
+  while (!(suspend_ns ? mbar_try_wait_suspend(bar, parity, suspend_ns) : mbar_try_wait(bar, parity))) {
+    if ((++n & 63u) == 0 || suspend_ns) {
       if (*abort) return false;
       if (clock64() - t0 > SF_WAIT_CYCLES) {
         *abort = 1;
@@ -99,6 +112,17 @@ SF_DEVICE bool mbar_wait_drain(uint64_t *bar, uint32_t parity) {
 
 SF_DEVICE void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Plain shared-memory accesses by 32-bit shared-window address.
+SF_DEVICE uint32_t lds32(uint32_t addr) {
+  uint32_t v;
+  asm volatile("ld.shared.b32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+  return v;
+}
+SF_DEVICE void sts128(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+  asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d)
+               : "memory");
 }
 
 SF_DEVICE void named_bar_sync(uint32_t id, uint32_t nthreads) {
@@ -188,6 +212,18 @@ SF_DEVICE void umma_f16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint3
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
       "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// umma_f16 issued only when `issue` is nonzero (a predicate, not a branch).
+SF_DEVICE void umma_f16_if(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                           uint32_t accumulate, uint32_t issue) {
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "setp.ne.b32 q, %5, 0;\n\t"
+      "@q tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate), "r"(issue)
       : "memory");
 }
 

@@ -2,28 +2,36 @@
 // voltages in the packet layout.
 //
 // One persistent CTA per SM streams each channel's packets once through
-// shared memory and builds fp16 operand tiles A[u][t] (row u = 2k + comp,
-// k = pol * R + receiver; 64 samples t per 128-byte row, 128-byte swizzle).
-// From the same tiles it can
-//   * correlate: G = A A^T with tcgen05 UMMA (A K-major), fp32 accumulation in
-//     tensor memory, drained every 512 samples into int32 running sums -> exact
-//     int32 visibilities in the trimmed packed-triangle layout.  Replaces the
-//     reference's fp16 ingest + layout permutations + Tensor Core Correlator +
-//     trim (include/spatial/spatial.cuh:55-304, lambda_gpu_pipeline.hpp:640-671,
+// shared memory and builds, per 128 samples, one fp16 operand tile
+//   X[t][u],  u = 4 r + 2 pol + comp   (receiver r, polarization, re/im)
+// i.e. the packet's own byte order: for every sample the 4R values of the
+// channel are contiguous.  The tile is stored as 64-value atoms
+// [atom][t][128 bytes] with the 128-byte swizzle, so the tensor cores read it
+//   * MN-major for the Gram G = X^T X (M/N = u, K = t), and
+//   * K-major for the beamformer Y[t][n] = sum_u X[t][u] W[n][u] (M = t, K = u).
+// Converting is then a straight element-wise int8 -> fp16 (x * scale) copy:
+// one lane = one sample, two receivers, one 16-byte store.
+//
+//   * correlate: G accumulates in fp32 in tensor memory and is drained every
+//     1024 samples into int32 running sums -> exact int32 visibilities in the
+//     trimmed packed-triangle layout.  Replaces the reference's fp16 ingest +
+//     layout permutations + Tensor Core Correlator + trim
+//     (include/spatial/spatial.cuh:55-304, lambda_gpu_pipeline.hpp:640-671,
 //     src/spatial.cu:176-200).
 //       Re V(k,m) = G[2k][2m] + G[2k+1][2m+1],  Im V(k,m) = G[2k+1][2m] - G[2k][2m+1]
-//     Rows 0..127 of G come from one M=128 x N=NR MMA; rows 128..NR-1 x columns
-//     128..NR-1 from a second M=128 x N=NR-128 MMA; the rest is V(k,m) = conj(V(m,k)).
-//   * beamform: Y^T[t][n] = sum_u A^T[t][u] W[n][u] per 128 samples, A read
-//     MN-major (two 64-sample tiles side by side), W the block-diagonal real
-//     form of the effective weights (n = pol, beam, re/im), fp32 accumulation,
-//     fp16 output [C][Pol][NB][T][2].  Replaces the reference's
-//     col-major sample layout + weight permutation + ccglib GEMM + half output
-//     (spatial.cuh:145-213, 376-418; lambda_gpu_pipeline.hpp:708-743).
+//     with k = 2 r + pol.  Rows 0..127 of G come from one M=128 x N=NR MMA,
+//     rows and columns 128..NR-1 from an M=64 MMA over the third atom; the
+//     rest is V(k,m) = conj(V(m,k)).
+//   * beamform: Y[t][n] per 128 samples, W the block-diagonal real form of the
+//     effective weights (n = pol, beam, re/im), fp32 accumulation, fp16 output
+//     [C][Pol][NB][T][2].  Replaces the reference's col-major sample layout +
+//     weight permutation + ccglib GEMM + half output (spatial.cuh:145-213,
+//     376-418; lambda_gpu_pipeline.hpp:708-743).
 //   * or both in one pass (the plain pipelines).
 // Operands: fp16(x * scale) is exact for |x s| <= 2048 and equals the
 // reference's ingest for unit gain; correlation chunks are exact while
-// |partial sums| <= 2^24 (512 samples of |x s| <= 128).
+// |partial sums| <= 2^24 (1024 samples of |x s| <= 128: every product of two
+// int8 values is at most 2^14 in magnitude).
 //
 // CTA roles (16 warps):
 //   warp 0           producer: one bulk (TMA) copy per packet [F][Tp][Rpp][Pol][2]
@@ -42,21 +50,27 @@
 
 namespace {
 
-constexpr int KBLK = 64;        // samples per K block = one 128-byte fp16 row
-constexpr int CHUNK_KBLK = 8;   // K blocks per exact fp32 chunk (512 samples)
-constexpr int NUM_OP_STAGES = 4;
+constexpr int KBLK = 64;         // samples per K block (chunk accounting)
+constexpr int TILE_T = 128;      // samples per operand stage
+constexpr uint32_t ATOM_BYTES = TILE_T * 128;  // one 64-value atom of a stage
+constexpr int CHUNK_KBLK = 16;   // K blocks per exact fp32 chunk (1024 samples)
+constexpr int NUM_OP_STAGES = 2;
 constexpr int NUM_WARPS = 16;
 constexpr int NTHREADS = NUM_WARPS * 32;
 constexpr int WARP_TMA = 0;
 constexpr int WARP_MMA = 1;
 constexpr int WARP_EPI0 = 4;
 constexpr int WARP_CONV0 = 8;  // converters: warps 2-3 and 8-15
-constexpr int NUM_CONV_THREADS = 10 * 32;
+constexpr int NUM_CONV_WARPS = 10;
+constexpr int NUM_CONV_THREADS = NUM_CONV_WARPS * 32;
 constexpr int MAX_SLOTS = 32;
 constexpr int MAX_F = 64;
 constexpr uint32_t HEADER_BYTES = 2048;
 constexpr int MAX_R = 48;
 constexpr int MAX_BEAM_OUT = 16;  // beams (all slots) per pol in the tensor beamformer
+// receiver pairs (16-byte chunks of a sample) one converter warp owns at most
+constexpr int MAX_JP = (MAX_R / 2 + NUM_CONV_WARPS - 1) / NUM_CONV_WARPS;
+constexpr uint32_t SUSPEND_NS = 20000;  // mbarrier suspend hint for waits off the MMA path
 
 struct CorrArgs {
   const int8_t *samples;
@@ -67,12 +81,13 @@ struct CorrArgs {
   __half2 *beams;      // [C][2][NB][T]
   uint32_t *status;
   int C, F, Tp, R, Rpp, P, T, NBL;
-  int NR;           // operand rows holding data: round_up(4R, 16)
-  int stage_rows;   // rows per operand stage: max(NR, 128)
-  int nkb;          // K blocks per channel (even when beamforming)
+  int NR;           // Gram rows/columns holding data: round_up(4R, 16)
+  int natoms;       // 64-value atoms per operand stage: max(2, ceil(NR / 64))
+  int nkb;          // K blocks per channel (even: stages hold two)
   int slot_bytes;   // one packet of one channel: R * Tp * 4 bytes
   int slot_stride;  // slot_bytes + the packet's scales, rounded to 16
   int num_slots;    // packet ring depth (power of two)
+  uint32_t tp_magic;  // ceil(2^32 / Tp): q / Tp == umulhi(q, tp_magic) while q * Tp < 2^32
   int NB, NBW;      // beams written per pol; rows of weff per (c, p)
   int BN;           // beam MMA N = round_up(4 NB, 16)
   int katoms;       // 64-column K atoms of the weight tile: ceil(NR / 64)
@@ -97,6 +112,9 @@ struct __align__(8) Header {
   uint32_t tmem_base;
   int abort;
   int offsets[MAX_F];
+  int rx_off[MAX_R];   // byte offset of receiver r's word at packet time 0 within a slot
+  int rx_woff[MAX_R];  // window offset (samples) of receiver r's FPGA
+  uint32_t unit_bits[2];  // per stage parity: bit s = ring slot s holds a packet whose scales are all 1
 };
 static_assert(sizeof(Header) <= HEADER_BYTES, "header too large");
 
@@ -139,7 +157,9 @@ __device__ __forceinline__ void emit_vis(const CorrArgs &a, int c, int p, int i,
   a.vis[idx] = val;
 }
 
-// Shared-memory descriptor with explicit strides (128-byte swizzle).
+// Shared-memory descriptor with explicit strides (128-byte swizzle).  K-major:
+// lbo unused, sbo = 8-row group stride.  MN-major: lbo = stride between
+// 64-value MN atoms, sbo = stride between 8-row K groups.
 __device__ __forceinline__ uint64_t desc_sw128(uint32_t addr, uint32_t lbo, uint32_t sbo) {
   uint64_t d = 0;
   d |= static_cast<uint64_t>((addr >> 4) & 0x3FFFu);
@@ -150,7 +170,9 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t addr, uint32_t lbo, uint
   return d;
 }
 
-template <bool DO_CORR, bool DO_BEAM>
+// tcgen05.mma issue is serialised with the issuing thread's own instruction
+// stream, so the issue loops below are straight-line: no branch between MMAs.
+template <bool DO_CORR, bool DO_BEAM, bool CORNER>
 __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   Header &h = *reinterpret_cast<Header *>(smem);
@@ -161,7 +183,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
   const uint32_t sbase = smem_u32(smem);
   const uint32_t op_addr = (sbase + HEADER_BYTES + 1023u) & ~1023u;
   uint8_t *op_ptr = smem + (op_addr - sbase);
-  const uint32_t stage_bytes = static_cast<uint32_t>(a.stage_rows) * 128u;
+  const uint32_t stage_bytes = static_cast<uint32_t>(a.natoms) * ATOM_BYTES;
   const uint32_t w_addr = op_addr + NUM_OP_STAGES * stage_bytes;  // weight tiles (1024-aligned)
   uint8_t *w_ptr = op_ptr + NUM_OP_STAGES * stage_bytes;
   uint8_t *ring_ptr = w_ptr + (DO_BEAM ? 2 * a.wtile_bytes : 0u);
@@ -172,10 +194,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
   if (tid == 0) {
     for (int s = 0; s < NS; ++s) {
       mbar_init(&h.pk_full[s], 1 + 32);
-      mbar_init(&h.pk_empty[s], 1);
+      mbar_init(&h.pk_empty[s], NUM_CONV_WARPS);
     }
     for (int s = 0; s < NUM_OP_STAGES; ++s) {
-      mbar_init(&h.op_full[s], 1);
+      mbar_init(&h.op_full[s], NUM_CONV_WARPS);
       mbar_init(&h.op_empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -185,7 +207,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     for (int b = 0; b < 2; ++b) {
       mbar_init(&h.beam_full[b], 1);
       mbar_init(&h.beam_empty[b], 4);
-      mbar_init(&h.w_full[b], 1);
+      mbar_init(&h.w_full[b], NUM_CONV_WARPS);
       mbar_init(&h.w_empty[b], 1);
     }
     mbar_init(&h.mma_done, 1);
@@ -193,7 +215,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     fence_mbarrier_init();
   }
   for (int f = tid; f < a.F; f += NTHREADS) h.offsets[f] = a.offsets[f];
-  // Padding rows/columns of the operand and weight tiles must read as zero.
+  for (int r = tid; r < a.R; r += NTHREADS) {
+    const int f = r / a.Rpp;
+    h.rx_off[r] = (f * a.Tp * a.Rpp + (r - f * a.Rpp)) * 4;
+    h.rx_woff[r] = a.offsets[f];
+  }
+  // Rows of the operand tiles past 4R and padding of the weight tiles must
+  // read as zero; the converters never write them.
   {
     uint4 *z = reinterpret_cast<uint4 *>(op_ptr);
     const int n16 = (NUM_OP_STAGES * stage_bytes + (DO_BEAM ? 2 * a.wtile_bytes : 0u)) / 16;
@@ -218,6 +246,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
   const int qbN = min(a.P + 1, (T - 1 + off_max) / Tp);
   const int npk = qbN - qa0 + 1;
   const int nchunks = (a.nkb + CHUNK_KBLK - 1) / CHUNK_KBLK;
+  const int npairs = a.nkb >> 1;
   volatile int *abort_flag = &h.abort;
 
   if (warp == WARP_TMA) {
@@ -229,7 +258,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
       const int16_t *chan_sc = a.scales + (size_t)c * (a.P + 2) * R * 2;
       for (int q = qa0; q <= qbN; ++q) {
         const uint32_t slot = g & ns_mask;
-        const bool ok = mbar_wait(&h.pk_empty[slot], ((g >> ns_shift) & 1u) ^ 1u, abort_flag, 64);
+        const bool ok = mbar_wait(&h.pk_empty[slot], ((g >> ns_shift) & 1u) ^ 1u, abort_flag, 20000);
         if (__any_sync(0xffffffffu, !ok)) {
           stop = true;
           break;
@@ -257,71 +286,78 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     if (lane == 0) {
       const uint32_t tmem = h.tmem_base;
       const int NR = a.NR;
-      const bool corner = NR > 128;
-      const uint32_t idesc_main = umma_idesc_f16_f32(128, NR);
-      // rows 128..NR-1 come from an M=64 MMA over rows NR-64..NR-1 (its
+      // Gram: A and B both the operand tile read MN-major
+      const uint32_t mn_major = (1u << 15) | (1u << 16);
+      const uint32_t idesc_main = umma_idesc_f16_f32(128, NR) | mn_major;
+      // rows/columns 128..NR-1: an M=64 MMA over the third atom (its
       // accumulator rows l sit in lanes (l % 16) + 32 (l / 16))
-      const uint32_t idesc_corner = umma_idesc_f16_f32(64, corner ? NR - 128 : 16);
-      // beam: A (samples) MN-major, B (weights) K-major, M = 128 samples, N = BN
-      const uint32_t idesc_beam = umma_idesc_f16_f32(128, a.BN) | (1u << 15);
+      const uint32_t idesc_corner = umma_idesc_f16_f32(64, CORNER ? NR - 128 : 16) | mn_major;
+      const int nks = NR / 16;  // beam K steps (predicated, at most MAX_R / 4)
+      // beam: A = the same tile read K-major (M = 128 samples), B = weights K-major
+      const uint32_t idesc_beam = umma_idesc_f16_f32(128, a.BN);
+      // descriptors at offset 0; an offset adds (bytes >> 4) to the start field
+      const uint64_t d_mn0 = desc_sw128(op_addr, ATOM_BYTES, 1024);
+      const uint64_t d_k0 = desc_sw128(op_addr, 16, 1024);
+      const uint64_t d_w0 = desc_sw128(w_addr, 16, 1024);
       uint32_t op_iter = 0, acc_iter = 0, beam_iter = 0, cw = 0;
       bool failed = false;
       for (int c = blockIdx.x; c < a.C; c += gridDim.x, ++cw) {
         const uint32_t wb = cw & 1u;
-        if (DO_BEAM) failed |= !mbar_wait(&h.w_full[wb], (cw >> 1) & 1u, abort_flag);
-        for (int kb = 0; kb < a.nkb; ++kb) {
-          const uint32_t st = op_iter % NUM_OP_STAGES;
-          bool ok = mbar_wait(&h.op_full[st], (op_iter / NUM_OP_STAGES) & 1u, abort_flag);
-          const bool chunk_start = (kb % CHUNK_KBLK) == 0;
-          const uint32_t abuf = acc_iter % a.nacc;
-          if (DO_CORR && chunk_start)
-            ok = mbar_wait(&h.acc_empty[abuf], ((acc_iter / a.nacc) & 1u) ^ 1u, abort_flag) && ok;
-          const bool beam_now = DO_BEAM && (kb & 1);
-          if (beam_now)
-            ok = mbar_wait(&h.beam_empty[beam_iter & 1u], ((beam_iter >> 1) & 1u) ^ 1u, abort_flag) && ok;
+        if (DO_BEAM) failed |= !mbar_wait(&h.w_full[wb], (cw >> 1) & 1u, abort_flag, SUSPEND_NS);
+        const uint32_t woff = wb * a.wtile_bytes;
+        for (int pr = 0; pr < npairs; ++pr) {
+          const uint32_t st = op_iter & 1u;
+          bool ok = mbar_wait(&h.op_full[st], (op_iter >> 1) & 1u, abort_flag, SUSPEND_NS);
           tc_fence_after();
-          if (ok) {
-            const uint32_t base = op_addr + st * stage_bytes;
-            if (DO_CORR) {
-              const uint32_t dacc = tmem + abuf * a.acc_stride;
+          const uint32_t soff = st * stage_bytes;
+          if (DO_CORR) {
+            // a chunk (CHUNK_KBLK K blocks) starts and ends on stage boundaries
+            const int kb0 = 2 * pr;
+            const bool chunk_start = (kb0 % CHUNK_KBLK) == 0;
+            const bool chunk_end = ((kb0 + 1) % CHUNK_KBLK) == CHUNK_KBLK - 1 || kb0 + 1 == a.nkb - 1;
+            const uint32_t abuf = acc_iter % a.nacc;
+            if (chunk_start) {
+              ok = mbar_wait(&h.acc_empty[abuf], ((acc_iter / a.nacc) & 1u) ^ 1u, abort_flag, SUSPEND_NS) && ok;
+              tc_fence_after();
+            }
+            failed |= !ok;
+            const uint32_t go = ok ? 1u : 0u;
+            const uint32_t dacc = tmem + abuf * a.acc_stride;
+            const uint64_t dst = d_mn0 + (soff >> 4);
+            // 8 K steps of 16 samples: K group pairs 2048 bytes apart
+            umma_f16_if(dacc, dst, dst, idesc_main, chunk_start ? 0u : 1u, go);
+            if (CORNER) umma_f16_if(dacc + NR, dst + (2 * ATOM_BYTES >> 4), dst + (2 * ATOM_BYTES >> 4), idesc_corner, chunk_start ? 0u : 1u, go);
 #pragma unroll
-              for (int ks = 0; ks < KBLK / 16; ++ks) {
-                const uint32_t acc = (!chunk_start || ks > 0) ? 1u : 0u;
-                umma_f16(dacc, umma_desc_sw128(base + ks * 32), umma_desc_sw128(base + ks * 32),
-                         idesc_main, acc);
-                if (corner)
-                  umma_f16(dacc + NR, umma_desc_sw128(base + (NR - 64) * 128 + ks * 32),
-                           umma_desc_sw128(base + 128 * 128 + ks * 32), idesc_corner, acc);
-              }
+            for (int ks = 1; ks < 2 * KBLK / 16; ++ks) {
+              const uint64_t dm = dst + (ks * 2048 >> 4);
+              umma_f16_if(dacc, dm, dm, idesc_main, 1u, go);
+              if (CORNER) umma_f16_if(dacc + NR, dm + (2 * ATOM_BYTES >> 4), dm + (2 * ATOM_BYTES >> 4), idesc_corner, 1u, go);
             }
-            if (beam_now) {
-              // the pair (st - 1, st): samples 0..63 and 64..127 of this tile
-              const uint32_t abase = base - stage_bytes;
-              const uint32_t wbase = w_addr + wb * a.wtile_bytes;
-              const uint32_t d = tmem + a.beam_off + (beam_iter & 1u) * a.BN;
-              for (int ks = 0; ks < NR / 16; ++ks) {
-                const uint64_t ad = desc_sw128(abase + ks * 16 * 128, stage_bytes, 1024);
-                const uint32_t kcol = ks * 16;
-                const uint64_t bd =
-                    desc_sw128(wbase + (kcol / 64) * (a.BN * 128) + (kcol % 64) * 2, 16, 1024);
-                umma_f16(d, ad, bd, idesc_beam, ks > 0 ? 1u : 0u);
-              }
+            if (chunk_end) {
+              umma_commit(&h.acc_full[abuf]);
+              ++acc_iter;
             }
-          } else {
-            failed = true;
           }
-          if (!DO_BEAM) {
-            umma_commit(&h.op_empty[st]);
-          } else if (kb & 1) {
-            umma_commit(&h.op_empty[(st + NUM_OP_STAGES - 1) % NUM_OP_STAGES]);
-            umma_commit(&h.op_empty[st]);
+          if (DO_BEAM) {
+            ok = mbar_wait(&h.beam_empty[beam_iter & 1u], ((beam_iter >> 1) & 1u) ^ 1u, abort_flag, SUSPEND_NS) && ok;
+            tc_fence_after();
+            failed |= !ok;
+            {
+              const uint32_t d = tmem + a.beam_off + (beam_iter & 1u) * a.BN;
+              const uint64_t ad0 = d_k0 + (soff >> 4);
+              const uint64_t bd0 = d_w0 + (woff >> 4);
+              const uint32_t batom = (a.BN * 128) >> 4;
+#pragma unroll
+              for (int ks = 0; ks < MAX_R / 4; ++ks) {
+                const uint32_t kof = ((ks & 3) * 32) >> 4;
+                umma_f16_if(d, ad0 + ((ks >> 2) * (ATOM_BYTES >> 4) + kof), bd0 + ((ks >> 2) * batom + kof),
+                            idesc_beam, ks > 0 ? 1u : 0u, (ok && ks < nks) ? 1u : 0u);
+              }
+            }
             umma_commit(&h.beam_full[beam_iter & 1u]);
             ++beam_iter;
           }
-          if (DO_CORR && ((kb % CHUNK_KBLK) == CHUNK_KBLK - 1 || kb == a.nkb - 1)) {
-            umma_commit(&h.acc_full[abuf]);
-            ++acc_iter;
-          }
+          umma_commit(&h.op_empty[st]);
           ++op_iter;
         }
         if (DO_BEAM) umma_commit(&h.w_empty[wb]);
@@ -337,29 +373,33 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     const int NR = a.NR;
     const int ncols = NR + (NR > 128 ? NR - 128 : 0);
     const int R4 = 4 * R;
+    const int ncplx = 2 * a.NB;  // beam output columns (pol, beam)
     uint32_t acc_iter = 0, beam_iter = 0;
     bool failed = false;
     for (int c = blockIdx.x; c < a.C; c += gridDim.x) {
       for (int kb = 0; kb < a.nkb; ++kb) {
         if (DO_BEAM && (kb & 1)) {
           const uint32_t buf = beam_iter & 1u;
-          const bool ok = mbar_wait(&h.beam_full[buf], (beam_iter >> 1) & 1u, abort_flag, 32);
+          const bool ok = mbar_wait(&h.beam_full[buf], (beam_iter >> 1) & 1u, abort_flag, 20000);
           failed |= !ok;
           tc_fence_after();
-          const int t = (kb >> 1) * 128 + ew * 32 + lane;
-          for (int cb = 0; cb < a.BN / 16; ++cb) {
-            uint32_t v[16];
-            tmem_ld16(tmem + a.beam_off + buf * a.BN + cb * 16, v);
+          const int t = (kb >> 1) * TILE_T + ew * 32 + lane;
+          const bool st_ok = ok && t < T;
+          // output column col = pol * NB + beam: Y[c][col][t]
+          __half2 *dst = a.beams + ((size_t)c * ncplx) * T + t;
+          const uint32_t tb = tmem + a.beam_off + buf * a.BN;
+          for (int cb = 0; cb < a.BN / 16; cb += 2) {
+            uint32_t v0[16], v1[16];
+            tmem_ld16(tb + cb * 16, v0);
+            if (cb + 1 < a.BN / 16) tmem_ld16(tb + cb * 16 + 16, v1);
             tmem_wait_ld();
-            if (ok && t < T) {
+            if (st_ok) {
+              __half2 *q = dst + (size_t)(cb * 8) * T;
 #pragma unroll
-              for (int e2 = 0; e2 < 8; ++e2) {
-                const int col = cb * 8 + e2;  // complex column (pol, beam)
-                const int p = col / a.NB;
-                const int m = col - p * a.NB;
-                if (p < 2)
-                  a.beams[(((size_t)c * 2 + p) * a.NB + m) * T + t] =
-                      __floats2half2_rn(__uint_as_float(v[2 * e2]), __uint_as_float(v[2 * e2 + 1]));
+              for (int e2 = 0; e2 < 16; ++e2) {
+                const uint32_t re = e2 < 8 ? v0[2 * e2] : v1[2 * e2 - 16];
+                const uint32_t im = e2 < 8 ? v0[2 * e2 + 1] : v1[2 * e2 - 15];
+                if (cb * 8 + e2 < ncplx) q[(size_t)e2 * T] = __floats2half2_rn(__uint_as_float(re), __uint_as_float(im));
               }
             }
           }
@@ -371,7 +411,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
         if (!DO_CORR || !((kb % CHUNK_KBLK) == CHUNK_KBLK - 1 || kb == a.nkb - 1)) continue;
         const int ch = kb / CHUNK_KBLK;
         const uint32_t abuf = acc_iter % a.nacc;
-        const bool ok = mbar_wait(&h.acc_full[abuf], (acc_iter / a.nacc) & 1u, abort_flag, 32);
+        const bool ok = mbar_wait(&h.acc_full[abuf], (acc_iter / a.nacc) & 1u, abort_flag, 20000);
         failed |= !ok;
         tc_fence_after();
         const bool first = ch == 0;
@@ -394,13 +434,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
             continue;
           }
           // Final chunk of this channel: combine (re, im) row pairs and write.
+          // Row/column u = 2k + comp, k = 2 r + pol.
           const bool main_region = cb * 16 < NR;
-          const int u = main_region ? ew * 32 + lane : (lane < 16 ? (NR - 64) + ew * 16 + lane : 1 << 20);
+          const int u = main_region ? ew * 32 + lane : (lane < 16 ? 128 + ew * 16 + lane : 1 << 20);
           const int k = u >> 1;
           const int comp = u & 1;
-          const int p = k / R;
-          const int i = k - p * R;
-          const bool row_ok = ok && u < R4 && (main_region || u >= 128);
+          const int p = k & 1;
+          const int i = k >> 1;
+          const bool row_ok = ok && u < R4;
           const int m0 = main_region ? cb * 8 : 64 + ((cb * 16 - NR) >> 1);
 #pragma unroll
           for (int e2 = 0; e2 < 8; ++e2) {
@@ -410,8 +451,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
             const int val = comp ? g0 - other : g0 + other;
             const int m = m0 + e2;
             if (!row_ok || 2 * m >= R4) continue;
-            const int q = m / R;
-            const int j = m - q * R;
+            const int q = m & 1;
+            const int j = m >> 1;
             if (i <= j) emit_vis(a, c, p, i, q, j, comp, val);
             // Rows m >= 64 are not main-tile rows: their entries with a main-tile
             // column come from here, conjugated.
@@ -428,16 +469,46 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     if (failed && lane == 0) atomicOr(a.status, SF_DEVERR_TIMEOUT_EPILOGUE);
   } else if (warp >= WARP_CONV0 || warp == 2 || warp == 3) {
     // ---------------- converters ----------------
-    const int ct = warp >= WARP_CONV0 ? (warp - WARP_CONV0 + 2) * 32 + lane : (warp - 2) * 32 + lane;
+    // One leader warp waits for the stage's packets and a free operand stage,
+    // flags packets whose scales are all 1, and releases the others through a
+    // hardware named barrier (no polling by the other nine warps).
+    const int cwp = warp >= WARP_CONV0 ? warp - WARP_CONV0 + 2 : warp - 2;  // 0..9
+    const int ct = cwp * 32 + lane;
+    const bool leader = cwp == NUM_CONV_WARPS - 1;
     uint32_t g_base = 0, op_iter = 0, cw = 0;
     bool failed = false;
-    const int Rpp4 = a.Rpp * 4;
+    const int nrp = (R + 1) >> 1;  // receiver pairs = 16-byte chunks per sample
+    const uint32_t Rpp4 = static_cast<uint32_t>(a.Rpp * 4);
+    const uint32_t sstride = static_cast<uint32_t>(a.slot_stride);
+    const uint32_t ring_s = smem_u32(ring_ptr);
+    const uint32_t op_s = smem_u32(op_ptr);
+    uint32_t unit_bits = 0;  // leader: bit s = slot s holds an all-unit-scale packet
+    // This warp owns receiver pairs jp = cwp + 10 k (rows u = 8 jp .. 8 jp + 7)
+    // for all 128 samples of a stage: lane = sample within each 32-sample group.
+    int woff0[MAX_JP];                   // window offset of the pair's first receiver
+    uint32_t roff0[MAX_JP], dr1[MAX_JP]; // word offset in a slot; second receiver's word - first's
+    uint32_t stoff[MAX_JP];              // this lane's 16-byte chunk in group 0 of a stage
+    bool same[MAX_JP], has1[MAX_JP];
+    int woff1[MAX_JP];
+#pragma unroll
+    for (int k = 0; k < MAX_JP; ++k) {
+      const int jp = min(cwp + NUM_CONV_WARPS * k, nrp - 1);
+      const int r0 = 2 * jp, r1 = min(2 * jp + 1, R - 1);
+      woff0[k] = h.rx_woff[r0];
+      woff1[k] = h.rx_woff[r1];
+      roff0[k] = h.rx_off[r0];
+      dr1[k] = static_cast<uint32_t>(h.rx_off[r1] - h.rx_off[r0]);
+      same[k] = woff1[k] == woff0[k];
+      has1[k] = 2 * jp + 1 < R;
+      stoff[k] = (jp >> 3) * ATOM_BYTES + lane * 128 + (((jp & 7) ^ (lane & 7)) << 4);
+    }
     for (int c = blockIdx.x; c < a.C; c += gridDim.x, ++cw) {
       if (DO_BEAM) {
-        // weight tile for this channel: B[n][u], n = (pol, beam, re/im), K-major,
-        // 128-byte swizzle, one [BN rows][64 cols] block per K atom
+        // weight tile for this channel: B[n][u], n = (pol, beam, re/im),
+        // u = (receiver, pol, re/im), K-major, 128-byte swizzle, one
+        // [BN rows][64 cols] block per K atom
         const uint32_t wb = cw & 1u;
-        const bool ok = mbar_wait(&h.w_empty[wb], ((cw >> 1) & 1u) ^ 1u, abort_flag);
+        const bool ok = mbar_wait(&h.w_empty[wb], ((cw >> 1) & 1u) ^ 1u, abort_flag, SUSPEND_NS);
         failed |= !ok;
         if (ok) {
           uint8_t *wt = w_ptr + wb * a.wtile_bytes;
@@ -456,10 +527,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
 #pragma unroll
               for (int dd = 0; dd < 2; ++dd) {
                 const int u = atom * 64 + cc * 8 + q * 2 + dd;
+                const int r = u >> 2, pu = (u >> 1) & 1, cu = u & 1;
                 float v = 0.0f;
-                const int ku = u >> 1, cu = u & 1;
-                if (pn < 2 && u < 4 * R && ku / R == pn) {
-                  const int r = ku - pn * R;
+                if (pn < 2 && u < 4 * R && pu == pn) {
                   const float2 w = a.weff[(((size_t)c * 2 + pn) * a.NBW + mn) * R + r];
                   v = cn == 0 ? (cu == 0 ? w.x : -w.y) : (cu == 0 ? w.y : w.x);
                 }
@@ -472,134 +542,110 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
           }
         }
         fence_proxy_async_smem();
-        named_bar_sync(1, NUM_CONV_THREADS);
-        if (ct == 0) mbar_arrive(&h.w_full[wb]);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&h.w_full[wb]);
       }
       int q_rel = qa0;   // next packet to release
-      int q_wait = qa0;  // next packet not yet waited for
-      // per-task packet/time cursor of the task's first sample, advanced by
-      // one K block (64 samples) at a time: no division in the loop
-      int cur_pkt[2], cur_tt[2];
-#pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        const int task = ct + j * NUM_CONV_THREADS;
-        const int r = (task >> 3) < R ? (task >> 3) : 0;
-        const int qq = (task & 7) * 8 + h.offsets[r / a.Rpp];
-        cur_pkt[j] = qq / Tp;
-        cur_tt[j] = qq - cur_pkt[j] * Tp;
-      }
-      for (int kb = 0; kb < a.nkb; kb += 2) {
-        const int s0 = kb * KBLK;
-        const int qb = s0 < T ? min(a.P + 1, (min(s0 + 2 * KBLK - 1, T - 1) + off_max) / Tp) : qbN;
-        bool ok = true;
-        for (; q_wait <= qb && ok; ++q_wait) {
-          const uint32_t gq = g_base + (q_wait - qa0);
-          ok = mbar_wait(&h.pk_full[gq & ns_mask], (gq >> ns_shift) & 1u, abort_flag);
+      int q_wait = qa0;  // next packet not yet waited for (leader)
+      const uint32_t gq0 = g_base - static_cast<uint32_t>(qa0);  // ring index of packet q: gq0 + q
+      for (int pr = 0; pr < npairs; ++pr) {
+        const int s0 = pr * TILE_T;
+        const uint32_t st = op_iter & 1u;
+        if (leader) {
+          const int qb = s0 < T ? min(a.P + 1, (min(s0 + TILE_T - 1, T - 1) + off_max) / Tp) : qbN;
+          bool ok = true;
+          for (; q_wait <= qb && ok; ++q_wait) {
+            const uint32_t gq = gq0 + q_wait;
+            const uint32_t sl = gq & ns_mask;
+            ok = mbar_wait(&h.pk_full[sl], (gq >> ns_shift) & 1u, abort_flag, SUSPEND_NS);
+            bool unit = true;
+            for (int r = lane; r < R; r += 32) unit &= lds32(ring_s + sl * sstride + a.slot_bytes + r * 4) == 0x00010001u;
+            unit = __all_sync(0xffffffffu, unit);
+            unit_bits = unit ? (unit_bits | (1u << sl)) : (unit_bits & ~(1u << sl));
+          }
+          ok = ok && mbar_wait(&h.op_empty[st], ((op_iter >> 1) & 1u) ^ 1u, abort_flag, SUSPEND_NS);
+          failed |= !ok;
+          if (lane == 0) h.unit_bits[op_iter & 1u] = ok ? unit_bits : 0xFFFFFFFFu;
+          if (!ok && lane == 0) *abort_flag = 1;
         }
-        const uint32_t st0 = op_iter % NUM_OP_STAGES;
-        const uint32_t st1 = (op_iter + 1) % NUM_OP_STAGES;
-        ok = ok && mbar_wait(&h.op_empty[st0], ((op_iter / NUM_OP_STAGES) & 1u) ^ 1u, abort_flag);
-        ok = ok && mbar_wait(&h.op_empty[st1], (((op_iter + 1) / NUM_OP_STAGES) & 1u) ^ 1u, abort_flag);
-        failed |= !ok;
-        const bool fast = (s0 + 2 * KBLK <= T) && Tp >= 8;
+        named_bar_sync(1, NUM_CONV_THREADS);
+        const bool ok = *abort_flag == 0;
+        const uint32_t ubits = *reinterpret_cast<volatile uint32_t *>(&h.unit_bits[op_iter & 1u]);
+        const uint32_t stage_s = op_s + st * stage_bytes;
+        if (ok) {
 #pragma unroll
-        for (int j = 0; j < 2; ++j) {
-          const int task = ct + j * NUM_CONV_THREADS;
-          if (ok && task < R * 8) {
-            const int oct = task & 7;
-            const int r = task >> 3;
-            const int f = r / a.Rpp;
-            const int n = r - f * a.Rpp;
-            const uint32_t fn_off = static_cast<uint32_t>((f * Tp) * Rpp4 + n * 4);
-            uint32_t word[2][8], scw[2][8];
+          for (int k = 0; k < MAX_JP; ++k) {
+            const int jp = cwp + NUM_CONV_WARPS * k;
+            if (jp >= nrp) break;
+            // loads of the four 32-sample groups first, then convert + store
+            uint32_t wd[4][2], sl[4][2];
+            bool unit = true;
 #pragma unroll
-            for (int b = 0; b < 2; ++b) {
-              // cursor of this block's first sample
-              int pkt = cur_pkt[j], tt = cur_tt[j];
-              if (b) {
-                tt += KBLK;
-                while (tt >= Tp) { tt -= Tp; ++pkt; }
+            for (int g = 0; g < 4; ++g) {
+              const int t = s0 + g * 32 + lane;
+              const bool valid = t < T;
+              uint32_t qq = static_cast<uint32_t>(t + woff0[k]);
+              uint32_t pkt = __umulhi(qq, a.tp_magic);
+              uint32_t tt = qq - pkt * static_cast<uint32_t>(Tp);
+              sl[g][0] = (gq0 + pkt) & ns_mask;
+              const uint32_t a0 = ring_s + sl[g][0] * sstride + roff0[k] + tt * Rpp4;
+              uint32_t a1 = a0 + dr1[k];
+              sl[g][1] = sl[g][0];
+              if (!same[k]) {
+                qq = static_cast<uint32_t>(t + woff1[k]);
+                pkt = __umulhi(qq, a.tp_magic);
+                tt = qq - pkt * static_cast<uint32_t>(Tp);
+                sl[g][1] = (gq0 + pkt) & ns_mask;
+                a1 = ring_s + sl[g][1] * sstride + roff0[k] + dr1[k] + tt * Rpp4;
               }
-              if (fast) {
-                const uint8_t *slot_a = ring_ptr + (size_t)((g_base + (pkt - qa0)) & ns_mask) * a.slot_stride;
-                const uint8_t *slot_b = ring_ptr + (size_t)((g_base + (pkt + 1 - qa0)) & ns_mask) * a.slot_stride;
-                const uint32_t sc_a = *reinterpret_cast<const uint32_t *>(slot_a + a.slot_bytes + r * 4);
-                const uint32_t sc_b = tt + 7 >= Tp
-                                          ? *reinterpret_cast<const uint32_t *>(slot_b + a.slot_bytes + r * 4)
-                                          : sc_a;
-#pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                  const int t = tt + e;
-                  const bool cross = t >= Tp;
-                  const uint8_t *sp = cross ? slot_b : slot_a;
-                  word[b][e] = *reinterpret_cast<const uint32_t *>(sp + fn_off + (cross ? t - Tp : t) * Rpp4);
-                  scw[b][e] = cross ? sc_b : sc_a;
-                }
-              } else {
-                const int sfirst = s0 + b * KBLK + oct * 8;
-#pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                  if (sfirst + e < T) {
-                    const uint8_t *slot_ptr = ring_ptr + (size_t)((g_base + (pkt - qa0)) & ns_mask) * a.slot_stride;
-                    word[b][e] = *reinterpret_cast<const uint32_t *>(slot_ptr + fn_off + tt * Rpp4);
-                    scw[b][e] = *reinterpret_cast<const uint32_t *>(slot_ptr + a.slot_bytes + r * 4);
-                  } else {
-                    word[b][e] = 0;
-                    scw[b][e] = 0;
-                  }
-                  if (++tt == Tp) {
-                    tt = 0;
-                    ++pkt;
-                  }
-                }
-              }
+              wd[g][0] = valid ? lds32(a0) : 0u;
+              wd[g][1] = valid && has1[k] ? lds32(a1) : 0u;
+              unit &= !valid || ((ubits >> sl[g][0]) & (ubits >> sl[g][1]) & 1u);
             }
+            if (__all_sync(0xffffffffu, unit)) {
+              // every scale is 1: x -> fp16(x) by the 1024 + b bias trick
 #pragma unroll
-            for (int b = 0; b < 2; ++b) {
-              uint32_t col[4][4];  // [row: p0re, p0im, p1re, p1im][pair of samples]
+              for (int g = 0; g < 4; ++g) {
+                uint32_t o[4];
 #pragma unroll
-              for (int e = 0; e < 8; e += 2) {
-                __half2 v0[2], v1[2];
-                convert_word(word[b][e], scw[b][e], v0[0], v1[0]);
-                convert_word(word[b][e + 1], scw[b][e + 1], v0[1], v1[1]);
-                col[0][e >> 1] = __byte_perm(u32_of(v0[0]), u32_of(v0[1]), 0x5410);
-                col[1][e >> 1] = __byte_perm(u32_of(v0[0]), u32_of(v0[1]), 0x7632);
-                col[2][e >> 1] = __byte_perm(u32_of(v1[0]), u32_of(v1[1]), 0x5410);
-                col[3][e >> 1] = __byte_perm(u32_of(v1[0]), u32_of(v1[1]), 0x7632);
+                for (int e = 0; e < 2; ++e) {
+                  const uint32_t biased = wd[g][e] ^ 0x80808080u;
+                  const __half2 bias = h2_of(0x64806480u);  // 1152
+                  o[2 * e] = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4140)), bias));
+                  o[2 * e + 1] = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4342)), bias));
+                }
+                sts128(stage_s + stoff[k] + g * (32 * 128), o[0], o[1], o[2], o[3]);
               }
-              uint8_t *stage = op_ptr + (b ? st1 : st0) * stage_bytes;
+            } else {
+              const int r0 = 2 * jp;
 #pragma unroll
-              for (int rr = 0; rr < 4; ++rr) {
-                const int pol = rr >> 1;
-                const int comp = rr & 1;
-                const int u = 2 * (pol * R + r) + comp;
-                uint4 *dst = reinterpret_cast<uint4 *>(stage + u * 128 + ((oct ^ (u & 7)) << 4));
-                *dst = make_uint4(col[rr][0], col[rr][1], col[rr][2], col[rr][3]);
+              for (int g = 0; g < 4; ++g) {
+                const bool valid = s0 + g * 32 + lane < T;
+                const uint32_t sc0 = valid ? lds32(ring_s + sl[g][0] * sstride + a.slot_bytes + r0 * 4) : 0x00010001u;
+                const uint32_t sc1 =
+                    valid && has1[k] ? lds32(ring_s + sl[g][1] * sstride + a.slot_bytes + r0 * 4 + 4) : 0x00010001u;
+                __half2 a0, a1, b0, b1;
+                convert_word(wd[g][0], sc0, a0, a1);
+                convert_word(wd[g][1], sc1, b0, b1);
+                sts128(stage_s + stoff[k] + g * (32 * 128), u32_of(a0), u32_of(a1), u32_of(b0), u32_of(b1));
               }
             }
           }
-          // advance the cursor by two K blocks
-          cur_tt[j] += 2 * KBLK;
-          while (cur_tt[j] >= Tp) { cur_tt[j] -= Tp; ++cur_pkt[j]; }
         }
         fence_proxy_async_smem();
-        named_bar_sync(1, NUM_CONV_THREADS);
-        // bookkeeping on the last converter thread
-        if (ct == NUM_CONV_THREADS - 1) {
-          mbar_arrive(&h.op_full[st0]);
-          mbar_arrive(&h.op_full[st1]);
+        __syncwarp();
+        if (lane == 0) {
+          mbar_arrive(&h.op_full[st]);
+          // packets no later stage needs go back to the producer
           int next = qbN + 1;
-          if (kb + 2 < a.nkb && (kb + 2) * KBLK < T) next = ((kb + 2) * KBLK + off_min) / Tp;
-          for (; q_rel < next; ++q_rel) {
-            const uint32_t gq = g_base + (q_rel - qa0);
-            mbar_arrive(&h.pk_empty[gq & ns_mask]);
-          }
+          if (pr + 1 < npairs && s0 + TILE_T < T) next = (s0 + TILE_T + off_min) / Tp;
+          for (; q_rel < next; ++q_rel) mbar_arrive(&h.pk_empty[(gq0 + q_rel) & ns_mask]);
         }
-        op_iter += 2;
+        ++op_iter;
       }
       g_base += npk;
     }
-    if (failed && ct == 0) atomicOr(a.status, SF_DEVERR_TIMEOUT_CONVERT);
+    if (failed && lane == 0) atomicOr(a.status, SF_DEVERR_TIMEOUT_CONVERT);
   }
 
   tc_fence_before();
@@ -611,19 +657,25 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
 }
 
 int g_max_smem = 0;
-bool g_attr_set[4] = {false, false, false, false};
+bool g_attr_set[8] = {false, false, false, false, false, false, false, false};
 
-template <bool DO_CORR, bool DO_BEAM>
+template <bool DO_CORR, bool DO_BEAM, bool CORNER>
 cudaError_t launch_mode(const CorrArgs &a, size_t smem, int grid, cudaStream_t stream) {
-  const int idx = (DO_CORR ? 1 : 0) + (DO_BEAM ? 2 : 0);
+  const int idx = (DO_CORR ? 1 : 0) + (DO_BEAM ? 2 : 0) + (CORNER ? 4 : 0);
   if (!g_attr_set[idx]) {
-    cudaError_t e = cudaFuncSetAttribute(sf_corrbeam_kernel<DO_CORR, DO_BEAM>,
+    cudaError_t e = cudaFuncSetAttribute(sf_corrbeam_kernel<DO_CORR, DO_BEAM, CORNER>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem);
     if (e != cudaSuccess) return e;
     g_attr_set[idx] = true;
   }
-  sf_corrbeam_kernel<DO_CORR, DO_BEAM><<<grid, NTHREADS, smem, stream>>>(a);
+  sf_corrbeam_kernel<DO_CORR, DO_BEAM, CORNER><<<grid, NTHREADS, smem, stream>>>(a);
   return cudaGetLastError();
+}
+
+template <bool DO_CORR, bool DO_BEAM>
+cudaError_t launch_corner(const CorrArgs &a, size_t smem, int grid, cudaStream_t stream) {
+  return a.NR > 128 ? launch_mode<DO_CORR, DO_BEAM, true>(a, smem, grid, stream)
+                    : launch_mode<DO_CORR, DO_BEAM, false>(a, smem, grid, stream);
 }
 
 uint32_t pow2_at_least(uint32_t x) {
@@ -642,11 +694,13 @@ int sf_correlate_supported(const sf_plan *p, char *why, size_t why_len) {
   if (p->R > MAX_R) return fail("correlator supports at most 48 receivers per channel");
   if (p->F > MAX_F) return fail("correlator supports at most 64 FPGAs");
   if ((p->R * p->Tp * 4) % 16 != 0) return fail("R * Tp must be a multiple of 4 (16-byte packets)");
+  // packet index by multiply-high: every window-shifted sample (< (P + 2) Tp) times Tp below 2^32
+  if ((double)(p->P + 2) * p->Tp * p->Tp >= 4294967296.0) return fail("integration too long for the packet index");
   return 1;
 }
 
 int sf_beam_tc_supported(const sf_plan *p, int n_beams_out) {
-  return p->R <= MAX_R && p->F <= MAX_F && (p->R * p->Tp * 4) % 16 == 0 && n_beams_out <= MAX_BEAM_OUT;
+  return sf_correlate_supported(p, nullptr, 0) && n_beams_out <= MAX_BEAM_OUT;
 }
 
 // mode bit 0: correlate, bit 1: beamform (n_beams_out beams per pol from the
@@ -672,10 +726,11 @@ cudaError_t sf_launch_corrbeam(const sf_plan *p, const int8_t *samples, const in
   a.T = p->T;
   a.NBL = p->NBL;
   a.NR = ((4 * p->R + 15) / 16) * 16;
-  a.stage_rows = std::max(a.NR, 128);
-  a.nkb = ((p->T + KBLK - 1) / KBLK + 1) & ~1;  // converters fill K blocks in pairs
+  a.natoms = std::max(2, (a.NR + 63) / 64);  // the M=128 Gram MMA always reads two atoms
+  a.nkb = ((p->T + KBLK - 1) / KBLK + 1) & ~1;  // stages hold K blocks in pairs
   a.slot_bytes = p->R * p->Tp * 4;
   a.slot_stride = a.slot_bytes + ((p->R * 4 + 15) / 16) * 16;
+  a.tp_magic = static_cast<uint32_t>((0x100000000ull + p->Tp - 1) / p->Tp);
   a.NB = n_beams_out;
   a.NBW = 2 * p->B;
   a.BN = ((4 * n_beams_out + 15) / 16) * 16;
@@ -709,8 +764,9 @@ cudaError_t sf_launch_corrbeam(const sf_plan *p, const int8_t *samples, const in
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&g_max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   }
-  const size_t fixed = HEADER_BYTES + 1024 + (size_t)NUM_OP_STAGES * a.stage_rows * 128 + 2 * a.wtile_bytes;
-  const int need_slots = 63 / p->Tp + 5;
+  const size_t fixed = HEADER_BYTES + 1024 + (size_t)NUM_OP_STAGES * a.natoms * ATOM_BYTES + 2 * a.wtile_bytes;
+  // packets one stage touches: (TILE_T - 1 + window spread <= 2 Tp) / Tp + 2, plus one in flight
+  const int need_slots = (TILE_T - 1) / p->Tp + 5;
   long avail = (long)g_max_smem - (long)fixed;
   int ns = avail > 0 ? (int)std::min<long>(MAX_SLOTS, avail / a.slot_stride) : 0;
   while (ns & (ns - 1)) ns &= ns - 1;  // round down to a power of two
@@ -718,9 +774,9 @@ cudaError_t sf_launch_corrbeam(const sf_plan *p, const int8_t *samples, const in
   a.num_slots = ns;
   const size_t smem = fixed + (size_t)ns * a.slot_stride;
   const int grid = std::max(1, std::min(p->C, p->num_sms));
-  if (do_corr && do_beam) return launch_mode<true, true>(a, smem, grid, stream);
-  if (do_corr) return launch_mode<true, false>(a, smem, grid, stream);
-  return launch_mode<false, true>(a, smem, grid, stream);
+  if (do_corr && do_beam) return launch_corner<true, true>(a, smem, grid, stream);
+  if (do_corr) return launch_corner<true, false>(a, smem, grid, stream);
+  return launch_corner<false, true>(a, smem, grid, stream);
 }
 
 cudaError_t sf_launch_correlate(const sf_plan *p, const int8_t *samples, const int16_t *scales,

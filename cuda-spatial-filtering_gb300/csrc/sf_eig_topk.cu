@@ -87,7 +87,7 @@ __device__ __forceinline__ int sturm_count(const float *d, const float *e2, int 
   if (fabsf(q) < pivmin) q = -pivmin;
   cnt += q < 0.0f;
   for (int i = 1; i < n; ++i) {
-    q = d[i] - x - e2[i - 1] / q;
+    q = d[i] - x - __fdividef(e2[i - 1], q);
     if (fabsf(q) < pivmin) q = -pivmin;
     cnt += q < 0.0f;
   }
@@ -243,9 +243,12 @@ __global__ void __launch_bounds__(WARPS * 32) sf_eig_topk_kernel(const TopkArgs 
   ghi += 2e-7f * tnorm + pivmin;
   for (int j = lane; j < n; j += 32) {
     float lo = glo, hi = ghi;
+    // absolute tolerance ~ float epsilon x ||T||, the accuracy any backward-
+    // stable solver reaches (and what detection and the shifts need)
+    const float atol = 2.4e-7f * tnorm + 4.0f * pivmin;
     for (int it = 0; it < 64; ++it) {
       const float mid = 0.5f * (lo + hi);
-      if (hi - lo <= 2.4e-7f * fmaxf(fabsf(lo), fabsf(hi)) + 4.0f * pivmin || mid == lo || mid == hi) break;
+      if (hi - lo <= atol || mid == lo || mid == hi) break;
       if (sturm_count(d, e2, n, mid, pivmin) > j) hi = mid;
       else lo = mid;
     }

@@ -117,7 +117,7 @@ def test_correlator_bit_exact_random(R, F, Tp, P, window, delays):
 
 def test_correlator_exact_at_full_scale():
     """Every sample at -128/127 over 4096 samples: partial sums reach 2^27, so
-    exactness relies on the 512-sample fp32 chunks drained into int32."""
+    exactness relies on the 1024-sample fp32 chunks drained into int32."""
     sh = orc.Shape(2, 4, 64, 36, 9, 64, 1)
     rng = np.random.default_rng(7)
     samples = np.where(rng.random(sh.samples_shape()) < 0.5, -128, 127).astype(np.int8)
