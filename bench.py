@@ -175,6 +175,26 @@ def measured_peaks():
     return 6800.0, 1900.0, "fallback"
 
 
+def max_over_ranks(ms, world, device):
+    """Slowest rank's elapsed time (every rank gets it), then a barrier: the
+    whole job ends when its last shard does."""
+    if world <= 1:
+        return float(ms)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def whole_job_value(ms_total, world, steps, channels):
+    """(ms per step, whole-job channel-integrations/s): every rank processes
+    its own shard of `channels` channels per step (weak scaling)."""
+    ms_per_step = ms_total / steps
+    return ms_per_step, world * channels / (ms_per_step / 1e3)
+
+
 def run_ours(args, world, rank):
     import torch
     import sfgb
@@ -225,14 +245,8 @@ def run_ours(args, world, rank):
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     torch.cuda.synchronize()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
-    ms_per_step = ms / args.steps
-    value = world * C / (ms_per_step / 1e3)
+    ms = max_over_ranks(ms, world, dev)
+    ms_per_step, value = whole_job_value(ms, world, args.steps, C)
 
     # per-kernel breakdown (stages launched one at a time on the same stream)
     kernels = _stage_breakdown(plan, d_s, d_sc, vis, ev, cnt, beams, stream, max(3, args.steps))
