@@ -175,6 +175,19 @@ def measured_peaks():
     return 6800.0, 1900.0, "fallback"
 
 
+def measured_traffic(kernel):
+    """DRAM bytes per launch of `kernel` on the 384-channel workload, from one
+    ncu capture summarised in profiles/traffic.txt (None when absent)."""
+    prof = ROOT / "profiles" / "traffic.txt"
+    if not prof.exists():
+        return None
+    for line in prof.read_text().splitlines():
+        parts = line.split()
+        if len(parts) == 2 and parts[0] == kernel:
+            return int(parts[1])
+    return None
+
+
 def max_over_ranks(ms, world, device):
     """Slowest rank's elapsed time (every rank gets it), then a barrier: the
     whole job ends when its last shard does."""
@@ -270,14 +283,7 @@ def run_ours(args, world, rank):
         roof = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "peak_source": peak_kind, "bytes_per_launch": byts,
                 "traffic": None, "note": "latency-bound eigensolver; matrices/s = %.0f" % (2 * C / (dom_ms / 1e3))}
-    prof = ROOT / "profiles" / "traffic.json"
-    if prof.exists():
-        try:
-            tr = json.loads(prof.read_text()).get(dom)
-            if tr:
-                roof["traffic"] = tr
-        except Exception:
-            pass
+    roof["traffic"] = measured_traffic(dom) if C == 384 else None
 
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
