@@ -129,6 +129,12 @@ SF_DEVICE void named_bar_sync(uint32_t id, uint32_t nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
+// Arrive on a named barrier without waiting for it (the waiting side uses
+// named_bar_sync with the same thread count).
+SF_DEVICE void named_bar_arrive(uint32_t id, uint32_t nthreads) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 // ---------------------------------------------------------------------------
 // Bulk async copy global -> shared (the non-tensor TMA path), completion on an
 // mbarrier transaction count.  Both addresses 16-byte aligned, size % 16 == 0.

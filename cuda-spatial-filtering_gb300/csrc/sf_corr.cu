@@ -61,15 +61,17 @@ constexpr int WARP_TMA = 0;
 constexpr int WARP_MMA = 1;
 constexpr int WARP_EPI0 = 4;
 constexpr int WARP_CONV0 = 8;  // converters: warps 2-3 and 8-15
-constexpr int NUM_CONV_WARPS = 10;
+constexpr int NUM_CONV_WARPS = 10;  // nine converting warps + one leader
 constexpr int NUM_CONV_THREADS = NUM_CONV_WARPS * 32;
+constexpr int NUM_WORKERS = NUM_CONV_WARPS - 1;  // warps that convert
+constexpr uint32_t BAR_START = 1, BAR_END = 2;  // named barriers of the converter group
 constexpr int MAX_SLOTS = 32;
 constexpr int MAX_F = 64;
 constexpr uint32_t HEADER_BYTES = 2048;
 constexpr int MAX_R = 48;
 constexpr int MAX_BEAM_OUT = 16;  // beams (all slots) per pol in the tensor beamformer
 // receiver pairs (16-byte chunks of a sample) one converter warp owns at most
-constexpr int MAX_JP = (MAX_R / 2 + NUM_CONV_WARPS - 1) / NUM_CONV_WARPS;
+constexpr int MAX_JP = (MAX_R / 2 + NUM_WORKERS - 1) / NUM_WORKERS;
 constexpr uint32_t SUSPEND_NS = 20000;  // mbarrier suspend hint for waits off the MMA path
 
 struct CorrArgs {
@@ -88,6 +90,7 @@ struct CorrArgs {
   int slot_stride;  // slot_bytes + the packet's scales, rounded to 16
   int num_slots;    // packet ring depth (power of two)
   uint32_t tp_magic;  // ceil(2^32 / Tp): q / Tp == umulhi(q, tp_magic) while q * Tp < 2^32
+  int prefetch;     // ring deep enough to hold a stage's packets and the next stage's
   int NB, NBW;      // beams written per pol; rows of weff per (c, p)
   int BN;           // beam MMA N = round_up(4 NB, 16)
   int katoms;       // 64-column K atoms of the weight tile: ceil(NR / 64)
@@ -194,10 +197,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
   if (tid == 0) {
     for (int s = 0; s < NS; ++s) {
       mbar_init(&h.pk_full[s], 1 + 32);
-      mbar_init(&h.pk_empty[s], NUM_CONV_WARPS);
+      mbar_init(&h.pk_empty[s], 1);
     }
     for (int s = 0; s < NUM_OP_STAGES; ++s) {
-      mbar_init(&h.op_full[s], NUM_CONV_WARPS);
+      mbar_init(&h.op_full[s], 1);
       mbar_init(&h.op_empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -385,27 +388,31 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
           tc_fence_after();
           const int t = (kb >> 1) * TILE_T + ew * 32 + lane;
           const bool st_ok = ok && t < T;
-          // output column col = pol * NB + beam: Y[c][col][t]
-          __half2 *dst = a.beams + ((size_t)c * ncplx) * T + t;
+          // the whole tile into registers, then the buffer goes back to the MMA
+          // before any global store (an arrive would wait for the stores)
           const uint32_t tb = tmem + a.beam_off + buf * a.BN;
-          for (int cb = 0; cb < a.BN / 16; cb += 2) {
-            uint32_t v0[16], v1[16];
-            tmem_ld16(tb + cb * 16, v0);
-            if (cb + 1 < a.BN / 16) tmem_ld16(tb + cb * 16 + 16, v1);
-            tmem_wait_ld();
-            if (st_ok) {
-              __half2 *q = dst + (size_t)(cb * 8) * T;
+          const int nblk = a.BN / 16;  // at most MAX_BEAM_OUT / 4
+          uint32_t v[MAX_BEAM_OUT / 4][16];
 #pragma unroll
-              for (int e2 = 0; e2 < 16; ++e2) {
-                const uint32_t re = e2 < 8 ? v0[2 * e2] : v1[2 * e2 - 16];
-                const uint32_t im = e2 < 8 ? v0[2 * e2 + 1] : v1[2 * e2 - 15];
-                if (cb * 8 + e2 < ncplx) q[(size_t)e2 * T] = __floats2half2_rn(__uint_as_float(re), __uint_as_float(im));
-              }
-            }
-          }
+          for (int cb = 0; cb < MAX_BEAM_OUT / 4; ++cb)
+            if (cb < nblk) tmem_ld16(tb + cb * 16, v[cb]);
+          tmem_wait_ld();
           tc_fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(&h.beam_empty[buf]);
+          if (st_ok) {
+            // output column col = pol * NB + beam: Y[c][col][t]
+            __half2 *dst = a.beams + ((size_t)c * ncplx) * T + t;
+#pragma unroll
+            for (int cb = 0; cb < MAX_BEAM_OUT / 4; ++cb) {
+#pragma unroll
+              for (int e2 = 0; e2 < 8; ++e2) {
+                const int col = cb * 8 + e2;
+                if (col < ncplx)
+                  dst[(size_t)col * T] = __floats2half2_rn(__uint_as_float(v[cb][2 * e2]), __uint_as_float(v[cb][2 * e2 + 1]));
+              }
+            }
+          }
           ++beam_iter;
         }
         if (!DO_CORR || !((kb % CHUNK_KBLK) == CHUNK_KBLK - 1 || kb == a.nkb - 1)) continue;
@@ -469,12 +476,15 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     if (failed && lane == 0) atomicOr(a.status, SF_DEVERR_TIMEOUT_EPILOGUE);
   } else if (warp >= WARP_CONV0 || warp == 2 || warp == 3) {
     // ---------------- converters ----------------
-    // One leader warp waits for the stage's packets and a free operand stage,
-    // flags packets whose scales are all 1, and releases the others through a
-    // hardware named barrier (no polling by the other nine warps).
+    // Nine warps convert; the leader warp acquires each stage's resources (the
+    // stage's packets, with a flag per packet whose scales are all 1, and a
+    // free operand stage) one stage ahead, opens the stage to the converters
+    // with a named barrier, collects their completion on a second one
+    // (converters only arrive), and then signals the MMA issuer and returns
+    // the packets no later stage needs.
     const int cwp = warp >= WARP_CONV0 ? warp - WARP_CONV0 + 2 : warp - 2;  // 0..9
     const int ct = cwp * 32 + lane;
-    const bool leader = cwp == NUM_CONV_WARPS - 1;
+    const bool leader = cwp == NUM_WORKERS;
     uint32_t g_base = 0, op_iter = 0, cw = 0;
     bool failed = false;
     const int nrp = (R + 1) >> 1;  // receiver pairs = 16-byte chunks per sample
@@ -482,8 +492,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     const uint32_t sstride = static_cast<uint32_t>(a.slot_stride);
     const uint32_t ring_s = smem_u32(ring_ptr);
     const uint32_t op_s = smem_u32(op_ptr);
-    uint32_t unit_bits = 0;  // leader: bit s = slot s holds an all-unit-scale packet
-    // This warp owns receiver pairs jp = cwp + 10 k (rows u = 8 jp .. 8 jp + 7)
+    // This warp owns receiver pairs jp = cwp + 9 k (rows u = 8 jp .. 8 jp + 7)
     // for all 128 samples of a stage: lane = sample within each 32-sample group.
     int woff0[MAX_JP];                   // window offset of the pair's first receiver
     uint32_t roff0[MAX_JP], dr1[MAX_JP]; // word offset in a slot; second receiver's word - first's
@@ -492,7 +501,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     int woff1[MAX_JP];
 #pragma unroll
     for (int k = 0; k < MAX_JP; ++k) {
-      const int jp = min(cwp + NUM_CONV_WARPS * k, nrp - 1);
+      const int jp = min(cwp + NUM_WORKERS * k, nrp - 1);
       const int r0 = 2 * jp, r1 = min(2 * jp + 1, R - 1);
       woff0[k] = h.rx_woff[r0];
       woff1[k] = h.rx_woff[r1];
@@ -502,6 +511,33 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
       has1[k] = 2 * jp + 1 < R;
       stoff[k] = (jp >> 3) * ATOM_BYTES + lane * 128 + (((jp & 7) ^ (lane & 7)) << 4);
     }
+    // leader state
+    uint32_t unit_bits = 0;  // bit s = ring slot s holds a packet whose scales are all 1
+    int q_rel = 0, q_wait = 0;
+    bool acq_ok = true;
+    // leader: wait for the packets of stage pr of the current channel and a
+    // free operand stage for op_iter_next; publish the packet flags
+    auto acquire = [&](int pr, uint32_t gq0, uint32_t it) {
+      const int s0 = pr * TILE_T;
+      const int qb = s0 < T ? min(a.P + 1, (min(s0 + TILE_T - 1, T - 1) + off_max) / Tp) : qbN;
+      bool ok = true;
+      for (; q_wait <= qb && ok; ++q_wait) {
+        const uint32_t gq = gq0 + q_wait;
+        const uint32_t sl = gq & ns_mask;
+        ok = mbar_wait(&h.pk_full[sl], (gq >> ns_shift) & 1u, abort_flag, SUSPEND_NS);
+        bool unit = true;
+        for (int r = lane; r < R; r += 32) unit &= lds32(ring_s + sl * sstride + a.slot_bytes + r * 4) == 0x00010001u;
+        unit = __all_sync(0xffffffffu, unit);
+        unit_bits = unit ? (unit_bits | (1u << sl)) : (unit_bits & ~(1u << sl));
+      }
+      ok = ok && mbar_wait(&h.op_empty[it & 1u], ((it >> 1) & 1u) ^ 1u, abort_flag, SUSPEND_NS);
+      if (lane == 0) h.unit_bits[it & 1u] = unit_bits;
+      if (!ok) {
+        failed = true;
+        if (lane == 0) *abort_flag = 1;
+      }
+      return ok;
+    };
     for (int c = blockIdx.x; c < a.C; c += gridDim.x, ++cw) {
       if (DO_BEAM) {
         // weight tile for this channel: B[n][u], n = (pol, beam, re/im),
@@ -545,106 +581,102 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
         __syncwarp();
         if (lane == 0) mbar_arrive(&h.w_full[wb]);
       }
-      int q_rel = qa0;   // next packet to release
-      int q_wait = qa0;  // next packet not yet waited for (leader)
       const uint32_t gq0 = g_base - static_cast<uint32_t>(qa0);  // ring index of packet q: gq0 + q
+      if (leader) {
+        q_rel = qa0;
+        q_wait = qa0;
+        acq_ok = acquire(0, gq0, op_iter);
+      }
       for (int pr = 0; pr < npairs; ++pr) {
         const int s0 = pr * TILE_T;
         const uint32_t st = op_iter & 1u;
+        named_bar_sync(BAR_START, NUM_CONV_THREADS);  // stage pr is open
         if (leader) {
-          const int qb = s0 < T ? min(a.P + 1, (min(s0 + TILE_T - 1, T - 1) + off_max) / Tp) : qbN;
-          bool ok = true;
-          for (; q_wait <= qb && ok; ++q_wait) {
-            const uint32_t gq = gq0 + q_wait;
-            const uint32_t sl = gq & ns_mask;
-            ok = mbar_wait(&h.pk_full[sl], (gq >> ns_shift) & 1u, abort_flag, SUSPEND_NS);
-            bool unit = true;
-            for (int r = lane; r < R; r += 32) unit &= lds32(ring_s + sl * sstride + a.slot_bytes + r * 4) == 0x00010001u;
-            unit = __all_sync(0xffffffffu, unit);
-            unit_bits = unit ? (unit_bits | (1u << sl)) : (unit_bits & ~(1u << sl));
+          // the next stage's resources while the converters work
+          const bool more = pr + 1 < npairs;
+          if (more && a.prefetch) acq_ok = acquire(pr + 1, gq0, op_iter + 1);
+          named_bar_sync(BAR_END, NUM_CONV_THREADS);  // every converter is done with stage pr
+          if (lane == 0) {
+            mbar_arrive(&h.op_full[st]);
+            // packets no later stage needs go back to the producer
+            int next = qbN + 1;
+            if (more && s0 + TILE_T < T) next = (s0 + TILE_T + off_min) / Tp;
+            for (; q_rel < next; ++q_rel) mbar_arrive(&h.pk_empty[(gq0 + q_rel) & ns_mask]);
           }
-          ok = ok && mbar_wait(&h.op_empty[st], ((op_iter >> 1) & 1u) ^ 1u, abort_flag, SUSPEND_NS);
-          failed |= !ok;
-          if (lane == 0) h.unit_bits[op_iter & 1u] = ok ? unit_bits : 0xFFFFFFFFu;
-          if (!ok && lane == 0) *abort_flag = 1;
-        }
-        named_bar_sync(1, NUM_CONV_THREADS);
-        const bool ok = *abort_flag == 0;
-        const uint32_t ubits = *reinterpret_cast<volatile uint32_t *>(&h.unit_bits[op_iter & 1u]);
-        const uint32_t stage_s = op_s + st * stage_bytes;
-        if (ok) {
+          __syncwarp();
+          if (more && !a.prefetch) acq_ok = acquire(pr + 1, gq0, op_iter + 1);
+        } else {
+          const bool ok = *abort_flag == 0;
+          const uint32_t ubits = *reinterpret_cast<volatile uint32_t *>(&h.unit_bits[st]);
+          const uint32_t stage_s = op_s + st * stage_bytes;
+          if (ok) {
 #pragma unroll
-          for (int k = 0; k < MAX_JP; ++k) {
-            const int jp = cwp + NUM_CONV_WARPS * k;
-            if (jp >= nrp) break;
-            // loads of the four 32-sample groups first, then convert + store
-            uint32_t wd[4][2], sl[4][2];
-            bool unit = true;
-#pragma unroll
-            for (int g = 0; g < 4; ++g) {
-              const int t = s0 + g * 32 + lane;
-              const bool valid = t < T;
-              uint32_t qq = static_cast<uint32_t>(t + woff0[k]);
-              uint32_t pkt = __umulhi(qq, a.tp_magic);
-              uint32_t tt = qq - pkt * static_cast<uint32_t>(Tp);
-              sl[g][0] = (gq0 + pkt) & ns_mask;
-              const uint32_t a0 = ring_s + sl[g][0] * sstride + roff0[k] + tt * Rpp4;
-              uint32_t a1 = a0 + dr1[k];
-              sl[g][1] = sl[g][0];
-              if (!same[k]) {
-                qq = static_cast<uint32_t>(t + woff1[k]);
-                pkt = __umulhi(qq, a.tp_magic);
-                tt = qq - pkt * static_cast<uint32_t>(Tp);
-                sl[g][1] = (gq0 + pkt) & ns_mask;
-                a1 = ring_s + sl[g][1] * sstride + roff0[k] + dr1[k] + tt * Rpp4;
-              }
-              wd[g][0] = valid ? lds32(a0) : 0u;
-              wd[g][1] = valid && has1[k] ? lds32(a1) : 0u;
-              unit &= !valid || ((ubits >> sl[g][0]) & (ubits >> sl[g][1]) & 1u);
-            }
-            if (__all_sync(0xffffffffu, unit)) {
-              // every scale is 1: x -> fp16(x) by the 1024 + b bias trick
+            for (int k = 0; k < MAX_JP; ++k) {
+              const int jp = cwp + NUM_WORKERS * k;
+              if (jp >= nrp) break;
+              // loads of the four 32-sample groups first, then convert + store
+              uint32_t wd[4][2], sl[4][2];
+              bool unit = true;
 #pragma unroll
               for (int g = 0; g < 4; ++g) {
-                uint32_t o[4];
-#pragma unroll
-                for (int e = 0; e < 2; ++e) {
-                  const uint32_t biased = wd[g][e] ^ 0x80808080u;
-                  const __half2 bias = h2_of(0x64806480u);  // 1152
-                  o[2 * e] = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4140)), bias));
-                  o[2 * e + 1] = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4342)), bias));
+                const int t = s0 + g * 32 + lane;
+                const bool valid = t < T;
+                uint32_t qq = static_cast<uint32_t>(t + woff0[k]);
+                uint32_t pkt = __umulhi(qq, a.tp_magic);
+                uint32_t tt = qq - pkt * static_cast<uint32_t>(Tp);
+                sl[g][0] = (gq0 + pkt) & ns_mask;
+                const uint32_t a0 = ring_s + sl[g][0] * sstride + roff0[k] + tt * Rpp4;
+                uint32_t a1 = a0 + dr1[k];
+                sl[g][1] = sl[g][0];
+                if (!same[k]) {
+                  qq = static_cast<uint32_t>(t + woff1[k]);
+                  pkt = __umulhi(qq, a.tp_magic);
+                  tt = qq - pkt * static_cast<uint32_t>(Tp);
+                  sl[g][1] = (gq0 + pkt) & ns_mask;
+                  a1 = ring_s + sl[g][1] * sstride + roff0[k] + dr1[k] + tt * Rpp4;
                 }
-                sts128(stage_s + stoff[k] + g * (32 * 128), o[0], o[1], o[2], o[3]);
+                wd[g][0] = valid ? lds32(a0) : 0u;
+                wd[g][1] = valid && has1[k] ? lds32(a1) : 0u;
+                unit &= !valid || ((ubits >> sl[g][0]) & (ubits >> sl[g][1]) & 1u);
               }
-            } else {
-              const int r0 = 2 * jp;
+              if (__all_sync(0xffffffffu, unit)) {
+                // every scale is 1: x -> fp16(x) by the 1024 + b bias trick
 #pragma unroll
-              for (int g = 0; g < 4; ++g) {
-                const bool valid = s0 + g * 32 + lane < T;
-                const uint32_t sc0 = valid ? lds32(ring_s + sl[g][0] * sstride + a.slot_bytes + r0 * 4) : 0x00010001u;
-                const uint32_t sc1 =
-                    valid && has1[k] ? lds32(ring_s + sl[g][1] * sstride + a.slot_bytes + r0 * 4 + 4) : 0x00010001u;
-                __half2 a0, a1, b0, b1;
-                convert_word(wd[g][0], sc0, a0, a1);
-                convert_word(wd[g][1], sc1, b0, b1);
-                sts128(stage_s + stoff[k] + g * (32 * 128), u32_of(a0), u32_of(a1), u32_of(b0), u32_of(b1));
+                for (int g = 0; g < 4; ++g) {
+                  uint32_t o[4];
+#pragma unroll
+                  for (int e = 0; e < 2; ++e) {
+                    const uint32_t biased = wd[g][e] ^ 0x80808080u;
+                    const __half2 bias = h2_of(0x64806480u);  // 1152
+                    o[2 * e] = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4140)), bias));
+                    o[2 * e + 1] = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4342)), bias));
+                  }
+                  sts128(stage_s + stoff[k] + g * (32 * 128), o[0], o[1], o[2], o[3]);
+                }
+              } else {
+                const int r0 = 2 * jp;
+#pragma unroll
+                for (int g = 0; g < 4; ++g) {
+                  const bool valid = s0 + g * 32 + lane < T;
+                  const uint32_t sc0 = valid ? lds32(ring_s + sl[g][0] * sstride + a.slot_bytes + r0 * 4) : 0x00010001u;
+                  const uint32_t sc1 =
+                      valid && has1[k] ? lds32(ring_s + sl[g][1] * sstride + a.slot_bytes + r0 * 4 + 4) : 0x00010001u;
+                  __half2 a0, a1, b0, b1;
+                  convert_word(wd[g][0], sc0, a0, a1);
+                  convert_word(wd[g][1], sc1, b0, b1);
+                  sts128(stage_s + stoff[k] + g * (32 * 128), u32_of(a0), u32_of(a1), u32_of(b0), u32_of(b1));
+                }
               }
             }
           }
-        }
-        fence_proxy_async_smem();
-        __syncwarp();
-        if (lane == 0) {
-          mbar_arrive(&h.op_full[st]);
-          // packets no later stage needs go back to the producer
-          int next = qbN + 1;
-          if (pr + 1 < npairs && s0 + TILE_T < T) next = (s0 + TILE_T + off_min) / Tp;
-          for (; q_rel < next; ++q_rel) mbar_arrive(&h.pk_empty[(gq0 + q_rel) & ns_mask]);
+          fence_proxy_async_smem();
+          named_bar_arrive(BAR_END, NUM_CONV_THREADS);  // done with stage pr
         }
         ++op_iter;
       }
       g_base += npk;
     }
+    (void)acq_ok;
     if (failed && lane == 0) atomicOr(a.status, SF_DEVERR_TIMEOUT_CONVERT);
   }
 
@@ -772,6 +804,7 @@ cudaError_t sf_launch_corrbeam(const sf_plan *p, const int8_t *samples, const in
   while (ns & (ns - 1)) ns &= ns - 1;  // round down to a power of two
   if (ns < need_slots) return cudaErrorInvalidConfiguration;
   a.num_slots = ns;
+  a.prefetch = ns >= (2 * TILE_T - 1) / p->Tp + 5 ? 1 : 0;
   const size_t smem = fixed + (size_t)ns * a.slot_stride;
   const int grid = std::max(1, std::min(p->C, p->num_sms));
   if (do_corr && do_beam) return launch_corner<true, true>(a, smem, grid, stream);
