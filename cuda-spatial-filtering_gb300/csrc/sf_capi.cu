@@ -45,6 +45,7 @@ void free_plan(sf_plan *p) {
   cudaFree(p->d_off_aligned);
   cudaFree(p->d_off_packet);
   cudaFree(p->d_factors);
+  cudaFree(p->d_perm);
   cudaFree(p->d_weights);
   cudaFree(p->d_weff);
   cudaFree(p->d_fixed_counts);
@@ -56,6 +57,7 @@ void free_plan(sf_plan *p) {
   free(p->h_gains);
   free(p->h_phasors);
   free(p->h_factors);
+  free(p->h_perm);
   free(p->h_fixed_counts);
   delete p;
 }
@@ -64,7 +66,13 @@ int upload_factors(sf_plan *p, cudaStream_t s) {
   for (int c = 0; c < p->C; ++c)
     for (int pol = 0; pol < 2; ++pol)
       for (int r = 0; r < p->R; ++r) {
-        const float2 g = p->h_gains[((size_t)c * 2 + pol) * p->R + r];
+        // the gain belongs to the source stream (applied at ingest), the
+        // phasor to the output receiver (applied after the reorder)
+        float2 g = p->h_gains[((size_t)c * 2 + pol) * p->R + r];
+        if (p->h_perm) {
+          const int32_t src = p->h_perm[2 * r + pol];
+          g = src < 0 ? make_float2(0.f, 0.f) : p->h_gains[((size_t)c * 2 + (src & 1)) * p->R + (src >> 1)];
+        }
         const float2 ph = p->h_phasors[(size_t)c * p->R + r];
         p->h_factors[((size_t)c * 2 + pol) * p->R + r] =
             make_float2(g.x * ph.x - g.y * ph.y, g.x * ph.y + g.y * ph.x);
@@ -253,6 +261,45 @@ int sf_set_fine_delays(sf_plan *plan, const float *h_delays_ns, double base_freq
   return SF_OK;
 }
 
+int sf_set_stream_permutation(sf_plan *plan, const int32_t *h_recv_perm, const int32_t *h_pol_perm,
+                              void *stream) {
+  if (int rc = check_plan(plan)) return rc;
+  const int R = plan->R;
+  cudaStream_t s = as_stream(stream);
+  if (!h_recv_perm && !h_pol_perm) {  // back to the identity
+    if (plan->d_perm) {
+      SF_TRY(cudaStreamSynchronize(s), "permutation reset");
+      cudaFree(plan->d_perm);
+      plan->d_perm = nullptr;
+    }
+    free(plan->h_perm);
+    plan->h_perm = nullptr;
+    if (int rc = upload_factors(plan, s)) return rc;
+    SF_TRY(cudaStreamSynchronize(s), "permutation reset");
+    return SF_OK;
+  }
+  if (!h_recv_perm || !h_pol_perm)
+    return set_err(SF_ERR_INVALID_ARGUMENT, "both permutation arrays are needed (or neither)");
+  for (int k = 0; k < 2 * R; ++k) {
+    if (h_recv_perm[k] < -1 || h_recv_perm[k] >= R)
+      return set_err(SF_ERR_INVALID_ARGUMENT, "recv_perm[%d] = %d outside [-1, %d)", k, h_recv_perm[k], R);
+    if (h_recv_perm[k] >= 0 && (h_pol_perm[k] < 0 || h_pol_perm[k] > 1))
+      return set_err(SF_ERR_INVALID_ARGUMENT, "pol_perm[%d] = %d is not 0 or 1", k, h_pol_perm[k]);
+  }
+  if (!plan->h_perm) {
+    plan->h_perm = static_cast<int32_t *>(malloc(sizeof(int32_t) * 2 * R));
+    if (!plan->h_perm) return set_err(SF_ERR_INVALID_ARGUMENT, "out of host memory");
+  }
+  for (int k = 0; k < 2 * R; ++k)
+    plan->h_perm[k] = h_recv_perm[k] < 0 ? -1 : ((h_recv_perm[k] << 1) | h_pol_perm[k]);
+  if (!plan->d_perm) SF_TRY(cudaMalloc(&plan->d_perm, sizeof(int32_t) * 2 * R), "cudaMalloc permutation");
+  SF_TRY(cudaMemcpyAsync(plan->d_perm, plan->h_perm, sizeof(int32_t) * 2 * R, cudaMemcpyHostToDevice, s),
+         "upload permutation");
+  if (int rc = upload_factors(plan, s)) return rc;
+  SF_TRY(cudaStreamSynchronize(s), "permutation upload");
+  return SF_OK;
+}
+
 int sf_set_weights(sf_plan *plan, const uint16_t *h_weights_f16, void *stream) {
   if (int rc = check_plan(plan)) return rc;
   if (!h_weights_f16) return set_err(SF_ERR_INVALID_ARGUMENT, "weights are NULL");
@@ -324,6 +371,8 @@ int sf_beamform(sf_plan *plan, const int8_t *d_samples, const int16_t *d_scales,
   if (window != SF_WINDOW_PACKET && window != SF_WINDOW_ALIGNED)
     return set_err(SF_ERR_INVALID_ARGUMENT, "unknown window %d", window);
   if (n_slots * plan->B > 32) return set_err(SF_ERR_UNSUPPORTED, "at most 32 output beams");
+  if (plan->d_perm && !sf_beam_tc_supported(plan, n_slots * plan->B))
+    return set_err(SF_ERR_UNSUPPORTED, "stream permutation with more than 16 output beams per pol");
   cudaStream_t s = as_stream(stream);
   if (n_slots == 1) SF_TRY(sf_launch_weights_plain(plan, s), "weights launch");
   const int32_t *off = window == SF_WINDOW_PACKET ? plan->d_off_packet : plan->d_off_aligned;

@@ -78,6 +78,7 @@ struct CorrArgs {
   const int8_t *samples;
   const int16_t *scales;
   const int32_t *offsets;
+  const int32_t *perm;  // [2R] stream permutation ((src_r << 1) | src_pol, -1 = zero), or NULL
   int32_t *vis;
   const float2 *weff;  // [C][2][NBW][R]
   __half2 *beams;      // [C][2][NB][T]
@@ -118,6 +119,7 @@ struct __align__(8) Header {
   int rx_off[MAX_R];   // byte offset of receiver r's word at packet time 0 within a slot
   int rx_woff[MAX_R];  // window offset (samples) of receiver r's FPGA
   uint32_t unit_bits[2];  // per stage parity: bit s = ring slot s holds a packet whose scales are all 1
+  int perm[2 * MAX_R];    // output stream 2 r + p <- source (src_r << 1) | src_pol, -1 = zero
 };
 static_assert(sizeof(Header) <= HEADER_BYTES, "header too large");
 
@@ -218,6 +220,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     fence_mbarrier_init();
   }
   for (int f = tid; f < a.F; f += NTHREADS) h.offsets[f] = a.offsets[f];
+  for (int k = tid; k < 2 * a.R; k += NTHREADS) h.perm[k] = a.perm ? a.perm[k] : ((k >> 1) << 1) | (k & 1);
   for (int r = tid; r < a.R; r += NTHREADS) {
     const int f = r / a.Rpp;
     h.rx_off[r] = (f * a.Tp * a.Rpp + (r - f * a.Rpp)) * 4;
@@ -609,7 +612,40 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
           const bool ok = *abort_flag == 0;
           const uint32_t ubits = *reinterpret_cast<volatile uint32_t *>(&h.unit_bits[st]);
           const uint32_t stage_s = op_s + st * stage_bytes;
-          if (ok) {
+          if (ok && a.perm) {
+            // permuted streams (reorder_streams semantics): every output stream
+            // of a chunk loads its own source receiver / pol with that source's
+            // FPGA window offset and packet scale
+#pragma unroll
+            for (int k = 0; k < MAX_JP; ++k) {
+              const int jp = cwp + NUM_WORKERS * k;
+              if (jp >= nrp) break;
+#pragma unroll 1
+              for (int g = 0; g < 4; ++g) {
+                const int t = s0 + g * 32 + lane;
+                uint32_t o[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                  const int r = 2 * jp + (e >> 1);
+                  const int src = r < R && t < T ? h.perm[2 * r + (e & 1)] : -1;
+                  float xr = 0.0f, xi = 0.0f;
+                  if (src >= 0) {
+                    const int sr = src >> 1, sp = src & 1;
+                    const uint32_t qq = static_cast<uint32_t>(t + h.rx_woff[sr]);
+                    const uint32_t pkt = __umulhi(qq, a.tp_magic);
+                    const uint32_t tt = qq - pkt * static_cast<uint32_t>(Tp);
+                    const uint32_t slot = ring_s + ((gq0 + pkt) & ns_mask) * sstride;
+                    const uint32_t raw = lds16(slot + h.rx_off[sr] + tt * Rpp4 + 2 * sp);
+                    const int sc = static_cast<int16_t>(lds16(slot + a.slot_bytes + sr * 4 + 2 * sp));
+                    xr = static_cast<float>(static_cast<int8_t>(raw & 0xFFu) * sc);
+                    xi = static_cast<float>(static_cast<int8_t>(raw >> 8) * sc);
+                  }
+                  o[e] = u32_of(__floats2half2_rn(xr, xi));  // fp16(x * scale)
+                }
+                sts128(stage_s + stoff[k] + g * (32 * 128), o[0], o[1], o[2], o[3]);
+              }
+            }
+          } else if (ok) {
 #pragma unroll
             for (int k = 0; k < MAX_JP; ++k) {
               const int jp = cwp + NUM_WORKERS * k;
@@ -745,6 +781,7 @@ cudaError_t sf_launch_corrbeam(const sf_plan *p, const int8_t *samples, const in
   a.samples = samples;
   a.scales = scales;
   a.offsets = offsets;
+  a.perm = p->d_perm;
   a.vis = vis;
   a.weff = p->d_weff;
   a.beams = beams;

@@ -33,6 +33,7 @@ constexpr int NW = NT / 32;
 constexpr int MAX_N = 64;
 constexpr int GROUP = 8;  // inverse-iteration vectors solved at once (one lane of warp 0 each)
 constexpr int INV_ITERS = 3;
+constexpr int MAX_B = 16;  // beams per pol handled by the projection step
 
 struct TopkArgs {
   const int32_t *vis;
@@ -60,6 +61,16 @@ __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
+}
+// Two independent sums reduced together (their shuffles overlap).
+__device__ __forceinline__ void warp_sum2(float &a, float &b) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float ta = __shfl_xor_sync(0xffffffffu, a, o);
+    const float tb = __shfl_xor_sync(0xffffffffu, b, o);
+    a += ta;
+    b += tb;
+  }
 }
 __device__ __forceinline__ float warp_max(float v) {
 #pragma unroll
@@ -242,8 +253,7 @@ __global__ void __launch_bounds__(NT) sf_eig_topk_kernel(const TopkArgs a) {
         dre = t.x;
         dim = t.y;
       }
-      dre = warp_sum(dre);
-      dim = warp_sum(dim);
+      warp_sum2(dre, dim);
       if (lane == 0) {
         s_red[(k & 1) * 2 * NW + warp] = dre;
         s_red[(k & 1) * 2 * NW + NW + warp] = dim;
@@ -412,8 +422,9 @@ __global__ void __launch_bounds__(NT) sf_eig_topk_kernel(const TopkArgs a) {
           const float ns = (i + 1 < n - 1) ? e[i + 1] : 0.0f;
           if (fabsf(cd) >= fabsf(sub)) {
             const float piv = fabsf(cd) < pert ? (cd < 0.0f ? -pert : pert) : cd;
-            const float l = sub / piv;
-            u0[i] = 1.0f / piv;
+            const float rp = 1.0f / piv;
+            const float l = sub * rp;
+            u0[i] = rp;
             u1[i] = cs;
             u2[i] = 0.0f;
             pv[i] = 0.0f;
@@ -440,20 +451,35 @@ __global__ void __launch_bounds__(NT) sf_eig_topk_kernel(const TopkArgs a) {
           const int r = g0 + lane;
           float *x = X + r * n;
           // forward: the row interchanges and multipliers of the factorisation
+          // (the running value stays in a register)
+          float cur = x[0];
           for (int i = 0; i < n - 1; ++i) {
-            float xi = x[i], xn = x[i + 1];
+            float nxt = x[i + 1];
             if (pv[i] != 0.0f) {
-              const float t = xi;
-              xi = xn;
-              xn = t;
+              const float t = cur;
+              cur = nxt;
+              nxt = t;
             }
-            x[i] = xi;
-            x[i + 1] = xn - ml[i] * xi;
+            x[i] = cur;
+            cur = nxt - ml[i] * cur;
           }
-          // back substitution
-          x[n - 1] = x[n - 1] * u0[n - 1];
-          if (n > 1) x[n - 2] = (x[n - 2] - u1[n - 2] * x[n - 1]) * u0[n - 2];
-          for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - u1[i] * x[i + 1] - u2[i] * x[i + 2]) * u0[i];
+          x[n - 1] = cur;
+          // back substitution, x[i+1] and x[i+2] carried in registers
+          float x1 = x[n - 1] * u0[n - 1];
+          x[n - 1] = x1;
+          float x2 = 0.0f;
+          if (n > 1) {
+            const float v = (x[n - 2] - u1[n - 2] * x1) * u0[n - 2];
+            x[n - 2] = v;
+            x2 = x1;
+            x1 = v;
+          }
+          for (int i = n - 3; i >= 0; --i) {
+            const float v = (x[i] - u1[i] * x1 - u2[i] * x2) * u0[i];
+            x[i] = v;
+            x2 = x1;
+            x1 = v;
+          }
           float s2 = 0.0f;
           for (int i = 0; i < n; ++i) s2 += x[i] * x[i];
           const float inv = s2 > 0.0f ? rsqrtf(s2) : 0.0f;
@@ -510,8 +536,7 @@ __global__ void __launch_bounds__(NT) sf_eig_topk_kernel(const TopkArgs a) {
           dre += t.x;
           dim += t.y;
         }
-        dre = warp_sum(dre);
-        dim = warp_sum(dim);
+        warp_sum2(dre, dim);
         const float2 s = cmul(tau, make_float2(dre, dim));
         for (int i = lane; i < m; i += 32) {
           const float2 v = i == 0 ? make_float2(1.0f, 0.0f) : A[(k + 1 + i) * ld + k];
@@ -537,17 +562,27 @@ __global__ void __launch_bounds__(NT) sf_eig_topk_kernel(const TopkArgs a) {
         for (int i = lane; i < n; i += 32) z[i] = make_float2(z[i].x * inv, z[i].y * inv);
       }
       __syncwarp();
-      // c_m = wgt (W_m . z)
-      for (int mm = 0; mm < B; ++mm) {
-        float cre = 0.0f, cim = 0.0f;
-        for (int i = lane; i < n; i += 32) {
-          const float2 t = cmul(__half22float2(w[mm * n + i]), z[i]);
-          cre += t.x;
-          cim += t.y;
+      // c_m = wgt (W_m . z): all partial sums first, then the reductions
+      {
+        float cre[MAX_B], cim[MAX_B];
+#pragma unroll
+        for (int mm = 0; mm < MAX_B; ++mm) {
+          cre[mm] = 0.0f;
+          cim[mm] = 0.0f;
+          if (mm < B)
+            for (int i = lane; i < n; i += 32) {
+              const float2 t = cmul(__half22float2(w[mm * n + i]), z[i]);
+              cre[mm] += t.x;
+              cim[mm] += t.y;
+            }
         }
-        cre = warp_sum(cre);
-        cim = warp_sum(cim);
-        if (lane == 0) coef[warp * B + mm] = make_float2(wgt * cre, wgt * cim);
+#pragma unroll
+        for (int mm = 0; mm < MAX_B; ++mm) {
+          if (mm < B) {
+            warp_sum2(cre[mm], cim[mm]);
+            if (lane == 0) coef[warp * B + mm] = make_float2(wgt * cre[mm], wgt * cim[mm]);
+          }
+        }
       }
     }
     __syncthreads();
@@ -577,7 +612,9 @@ __global__ void __launch_bounds__(NT) sf_eig_topk_kernel(const TopkArgs a) {
 
 size_t sf_eig_topk_smem(int n, int B) { return topk_floats(n, B) * sizeof(float); }
 
-int sf_eig_topk_supported(const sf_plan *p) { return p->R <= MAX_N && sf_eig_topk_smem(p->R, p->B) <= 200 * 1024; }
+int sf_eig_topk_supported(const sf_plan *p) {
+  return p->R <= MAX_N && p->B <= MAX_B && sf_eig_topk_smem(p->R, p->B) <= 200 * 1024;
+}
 
 cudaError_t sf_launch_eig_topk(const sf_plan *p, const int32_t *vis, int k_rule, float delta, int shrink,
                                float *evals, int32_t *counts, cudaStream_t stream) {

@@ -24,6 +24,12 @@ struct sf_plan {
   float2 *h_phasors;   // [C][R]
   float2 *h_factors;   // [C][2][R] staging for the upload
 
+  // Stream permutation (canonical output stream <- packet-order source), or
+  // identity when d_perm is NULL: entry k = 2 r + p holds (src_r << 1) | src_pol,
+  // -1 for a zero stream.
+  int32_t *d_perm;     // [2R]
+  int32_t *h_perm;     // [2R]
+
   __half2 *d_weights;  // [C][2][B][R]
   float2 *d_weff;      // [C][2][2B][R] effective weights for the beamformer
   int32_t *d_fixed_counts;  // [C]

@@ -60,6 +60,7 @@ _SIGS = {
     "sf_set_fine_delays": ([_P, _P, ctypes.c_double, ctypes.c_double, _I32, _P], ctypes.c_int),
     "sf_set_weights": ([_P, _P, _P], ctypes.c_int),
     "sf_set_fixed_counts": ([_P, _P, _P], ctypes.c_int),
+    "sf_set_stream_permutation": ([_P, _P, _P, _P], ctypes.c_int),
     "sf_correlate": ([_P, _P, _P, _I32, _P, _P], ctypes.c_int),
     "sf_covariance_eig": ([_P, _P, _I32, _I32, ctypes.c_float, _I32, _P, _P, _P, _P, _P], ctypes.c_int),
     "sf_beamform": ([_P, _P, _P, _I32, _I32, _P, _P], ctypes.c_int),
@@ -187,6 +188,19 @@ class Plan:
     def set_weights(self, weights_f16, stream=None):
         arr = np.ascontiguousarray(weights_f16, dtype=np.float16).reshape(self.C, 2, self.B, self.R, 2)
         _check(lib().sf_set_weights(self._h, arr.ctypes.data_as(_P), _stream(stream)))
+
+    def set_stream_permutation(self, recv_perm=None, pol_perm=None, stream=None):
+        """Canonical stream k = 2 r + p <- source receiver recv_perm[k] at pol
+        pol_perm[k] (-1 = zero); both None restores the identity."""
+        if recv_perm is None and pol_perm is None:
+            _check(lib().sf_set_stream_permutation(self._h, None, None, _stream(stream)))
+            return
+        rp = np.ascontiguousarray(recv_perm, dtype=np.int32).reshape(-1)
+        pp = np.ascontiguousarray(pol_perm, dtype=np.int32).reshape(-1)
+        if rp.size != 2 * self.R or pp.size != 2 * self.R:
+            raise ValueError("set_stream_permutation: size must equal 2 x receivers")
+        _check(lib().sf_set_stream_permutation(self._h, rp.ctypes.data_as(_P), pp.ctypes.data_as(_P),
+                                               _stream(stream)))
 
     def set_fixed_counts(self, counts=None, stream=None):
         arr = None if counts is None else np.ascontiguousarray(counts, dtype=np.int32)

@@ -1,8 +1,9 @@
 """Python mirrors of the reference's GPU stage interface over sf_capi.
 
 ``GPUPipeline`` mirrors include/spatial/pipeline_base.hpp:9-40 (same method
-names and argument meaning; ``set_stream_permutation`` raises like the base
-class); the three subclasses mirror the drop-in targets:
+names and argument meaning; ``set_stream_permutation`` as LambdaGPUPipeline's,
+lambda_gpu_pipeline.hpp:1139-1150); the three subclasses mirror the drop-in
+targets:
 
   LambdaCorrBeamOnlyGPUPipeline   lambda_corr_beam_only_gpu_pipeline.hpp:202-344
   LambdaGPUPipeline               lambda_gpu_pipeline.hpp:445-608
@@ -84,7 +85,11 @@ class GPUPipeline:
         self.plan.set_fine_delays(delays_ns, base_freq_hz, channel_bw_hz, min_freq_ch)
 
     def set_stream_permutation(self, recv_perm, pol_perm):
-        raise RuntimeError("set_stream_permutation not supported by this pipeline type")
+        # lambda_gpu_pipeline.hpp:1139-1150: sizes must be F * Rpp * Pol
+        if len(recv_perm) != 2 * self.plan.R or len(pol_perm) != 2 * self.plan.R:
+            raise RuntimeError("set_stream_permutation: size must equal NR_FPGA_SOURCES * "
+                               "NR_RECEIVERS_PER_PACKET * NR_POLARIZATIONS")
+        self.plan.set_stream_permutation(recv_perm, pol_perm)
 
     def execute_pipeline(self, packet_data, dummy_run=False):
         raise NotImplementedError

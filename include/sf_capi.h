@@ -114,6 +114,16 @@ int sf_set_antenna_gains(sf_plan *plan, const float *h_gains, void *stream);
 int sf_set_fine_delays(sf_plan *plan, const float *h_delays_ns, double base_freq_hz,
                        double channel_bw_hz, int32_t min_freq_ch, void *stream);
 
+/* GPUPipeline::set_stream_permutation (reference include/spatial/pipeline/lambda_gpu_pipeline.hpp:1139-1150,
+ * reorder_streams_kernel spatial.cuh:596-636): canonical output stream k = 2 r + p (receiver r,
+ * pol p) takes source receiver h_recv_perm[k] (flat f * Rpp + n, packet order) at source pol
+ * h_pol_perm[k]; h_recv_perm[k] = -1 gives a zero stream.  Both arrays have 2R entries; both NULL
+ * restores the identity.  Applied while the correlator/beamformer load their tiles (after the
+ * window alignment, as the reference); gains stay with the source stream, fine-delay phasors with
+ * the output receiver. */
+int sf_set_stream_permutation(sf_plan *plan, const int32_t *h_recv_perm, const int32_t *h_pol_perm,
+                              void *stream);
+
 /* Beam weights, BeamWeightsT<T> payload (reference include/spatial/pipeline/common.hpp:52-55). */
 int sf_set_weights(sf_plan *plan, const uint16_t *h_weights_f16, void *stream);
 

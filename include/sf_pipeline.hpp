@@ -17,8 +17,8 @@
  * FinalPacketData, Output and ProcessorStateBase (in the reference:
  * pipeline_base.hpp, packet_formats.hpp, output.hpp, spatial.hpp).  The
  * adapters use only their public / protected interface:
- *   GPUPipeline        state_, output_, the virtual set_* / execute_pipeline /
- *                      dump_visibilities
+ *   GPUPipeline        state_, output_, the virtual set_* (including
+ *                      set_stream_permutation) / execute_pipeline / dump_visibilities
  *   FinalPacketData    start_seq_id, end_seq_id, buffer_index, get_samples_ptr,
  *                      get_samples_elements_size, get_scales_ptr,
  *                      get_scales_element_size, get_arrivals_ptr,
@@ -202,6 +202,16 @@ template <typename Config, typename Base, int Mode> class SfPipelineBase : publi
     for (auto &b : buffers_)
       detail::check(sf_set_fine_delays(b->plan, delays_ns, base_freq_hz, channel_bw_hz, min_freq_ch, b->stream),
                     "sf_set_fine_delays");
+  }
+
+  // LambdaGPUPipeline::set_stream_permutation: both vectors F * Rpp * Pol long
+  void set_stream_permutation(const std::vector<int> &recv_perm, const std::vector<int> &pol_perm) override {
+    if ((int)recv_perm.size() != 2 * R || (int)pol_perm.size() != 2 * R)
+      throw std::runtime_error(
+          "set_stream_permutation: size must equal NR_FPGA_SOURCES * NR_RECEIVERS_PER_PACKET * NR_POLARIZATIONS");
+    std::vector<int32_t> rp(recv_perm.begin(), recv_perm.end()), pp(pol_perm.begin(), pol_perm.end());
+    for (auto &b : buffers_)
+      detail::check(sf_set_stream_permutation(b->plan, rp.data(), pp.data(), b->stream), "sf_set_stream_permutation");
   }
 
   void execute_pipeline(FinalPacketData *packet_data, const bool dummy_run = false) override {

@@ -132,6 +132,45 @@ def aligned_samples(shape, samples, scales, offsets):
     return re, im
 
 
+def permute_streams(shape, re, im, recv_perm, pol_perm):
+    """Canonical streams from the packet-order ones, after alignment
+    (reorder_streams_kernel, spatial.cuh:596-636; set_stream_permutation,
+    lambda_gpu_pipeline.hpp:1139-1150): output stream (receiver r, pol p),
+    index k = 2 r + p, is source receiver recv_perm[k] (flat f * Rpp + n) at
+    source pol pol_perm[k]; recv_perm[k] = -1 gives zeros."""
+    rp = np.asarray(recv_perm, np.int64).reshape(shape.R, NPOL)
+    pp = np.asarray(pol_perm, np.int64).reshape(shape.R, NPOL)
+    ore = np.zeros_like(re)
+    oim = np.zeros_like(im)
+    for r in range(shape.R):
+        for p in range(NPOL):
+            src = rp[r, p]
+            if src < 0:
+                continue
+            ore[:, p, r, :] = re[:, pp[r, p], src, :]
+            oim[:, p, r, :] = im[:, pp[r, p], src, :]
+    return ore, oim
+
+
+def permuted_factors(shape, recv_perm, pol_perm, gains=None, phasors=None):
+    """Per-output-stream factor d: the gain is applied at ingest to the source
+    stream (spatial.cuh:464-476), the fine-delay phasor after the reorder to the
+    output receiver (lambda_gpu_pipeline.hpp:680-701)."""
+    g = np.ones((shape.C, NPOL, shape.R), dtype=np.complex128)
+    if gains is not None:
+        g = np.asarray(gains, np.complex128).reshape(shape.C, NPOL, shape.R)
+    rp = np.asarray(recv_perm, np.int64).reshape(shape.R, NPOL)
+    pp = np.asarray(pol_perm, np.int64).reshape(shape.R, NPOL)
+    d = np.zeros((shape.C, NPOL, shape.R), dtype=np.complex128)
+    for r in range(shape.R):
+        for p in range(NPOL):
+            if rp[r, p] >= 0:
+                d[:, p, r] = g[:, pp[r, p], rp[r, p]]
+    if phasors is not None:
+        d = d * np.asarray(phasors, np.complex128).reshape(shape.C, 1, shape.R)
+    return d
+
+
 # --------------------------------------------------------------------------
 # Correlation (exact integers)
 # --------------------------------------------------------------------------
@@ -403,7 +442,7 @@ def lambda_gpu_chain(shape, samples, scales, weights, delays=None, d=None):
 
 
 def adaptive_chain(shape, samples, scales, weights, k_fixed=None, detect=False,
-                   delta=3.0, shrink=False, delays=None, d=None, k_rule=None):
+                   delta=3.0, shrink=False, delays=None, d=None, k_rule=None, perm=None):
     """Adaptive null/shrink chain
     (lambda_adaptive_beamformed_spectra_pipeline.hpp:563-798): per (c, p)
     same-polarisation covariance, diagonal whitening, eigendecomposition, K,
@@ -413,6 +452,8 @@ def adaptive_chain(shape, samples, scales, weights, k_fixed=None, detect=False,
     if d is None:
         d = receiver_factors(shape)
     re, im = aligned_samples(shape, samples, scales, offsets)
+    if perm is not None:  # (recv_perm, pol_perm): reorder after the alignment
+        re, im = permute_streams(shape, re, im, perm[0], perm[1])
     vis = correlate(shape, re, im)
     vc = scaled_visibilities(shape, vis, d)
     C, R, B = shape.C, shape.R, shape.B

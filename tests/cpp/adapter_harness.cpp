@@ -77,6 +77,9 @@ class GPUPipeline {
   virtual void set_subpacket_delays(int *delays_subpacket) { subpacket_delays_ = delays_subpacket; }
   virtual void set_antenna_gains(std::complex<float> *gains) { gains_ = gains; }
   virtual void set_fine_delays(const float *, double, double, int) {}
+  virtual void set_stream_permutation(const std::vector<int> &, const std::vector<int> &) {
+    throw std::runtime_error("set_stream_permutation not supported by this pipeline type");
+  }
   virtual void execute_pipeline(FinalPacketData *packet_data, const bool dummy_run = false) = 0;
   virtual void dump_visibilities(const uint64_t end_seq_num = 0) = 0;
 

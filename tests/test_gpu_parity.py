@@ -240,6 +240,37 @@ def test_adaptive_null_projection_and_beams(lambda_cfg):
             assert np.abs(U @ U.conj().T - Ur @ Ur.conj().T).max() <= 2e-3
 
 
+def test_plain_chain_at_golden_test_size():
+    """The plain chain at the reference's golden-test size: 36 antennas, 2 pols,
+    8 channels, 1024 samples (I, Q = clip(round(N(0, 16^2)), -127, 127), seed 0),
+    per-channel per-pol covariance, eigendecomposition, null the top k = 1
+    eigenvector, one beam with unit-modulus weights of uniform random phase."""
+    sh = orc.Shape(8, 4, 64, 36, 9, 16, 1)
+    samples, scales, _ = orc.synth_inputs(sh, seed=0)
+    rng = np.random.Generator(np.random.PCG64(0))
+    ph = rng.uniform(0.0, 2.0 * np.pi, size=(sh.C, 2, sh.B, sh.R))
+    weights = np.stack([np.cos(ph), np.sin(ph)], axis=-1).astype(np.float16)
+    fixed = np.ones(sh.C, np.int32)
+    got = _run_adaptive_gpu(sh, samples, scales, weights, sfgb.SF_K_FIXED, 0.0, fixed=fixed)
+    ref = orc.adaptive_chain(sh, samples, scales, weights, k_fixed=fixed)
+    assert np.array_equal(got["vis"], ref["vis"])  # int32 visibilities bit-exact
+    assert np.array_equal(got["counts"], np.ones((sh.C, 2), np.int32))
+    vc = orc.scaled_visibilities(sh, ref["vis"], orc.receiver_factors(sh))
+    for p in range(2):
+        m = orc.unpack_hermitian(sh, vc, p, p)
+        for c in range(sh.C):
+            assert np.all(np.real(np.diag(m[c])) >= 0)  # non-negative autocorrelations
+            assert np.allclose(m[c], m[c].conj().T)  # Hermitian covariance
+            a, _ = orc.whiten(m[c])
+            norm = np.linalg.norm(a, 2)
+            assert np.max(np.abs(got["evals"][c, p] - ref["evals"][c, p])) <= 2e-5 * norm
+    yr = ref["beams"]
+    yb = got["beams"][..., 0] + 1j * got["beams"][..., 1]
+    err = np.abs(yb - yr)
+    assert np.all(err[:, :, :sh.B] <= 2.0 ** -9 * np.abs(yr[:, :, :sh.B]) + 2.0 ** -6)
+    assert np.all(err <= 2.0 ** -9 * np.abs(yr) + 2.0 ** -6 + 1e-3 * np.abs(yr).max(axis=-1, keepdims=True))
+
+
 def test_adaptive_detection_counts_match_oracle(lambda_cfg):
     sh, samples, scales, weights, rfi = lambda_cfg
     got = _run_adaptive_gpu(sh, samples, scales, weights, sfgb.SF_K_DETECT, 3.0)
@@ -338,3 +369,107 @@ def test_reference_adaptive_goldens_topk_path(case):
     c2 = copy.copy(case)
     c2.expect = {k: v for k, v in e.items() if k not in ("evals", "principal_evec")}
     check_case(c2, out)
+
+
+# --------------------------------------------------------------------------
+# Stream permutation (reorder_streams, set_stream_permutation)
+# --------------------------------------------------------------------------
+def _random_stream_perm(sh, seed, n_zero=3):
+    rng = np.random.default_rng(seed)
+    src = rng.permutation(2 * sh.R)
+    recv = (src // 2).astype(np.int32)
+    pol = (src % 2).astype(np.int32)
+    recv[rng.choice(2 * sh.R, n_zero, replace=False)] = -1  # zero streams
+    recv[5] = recv[9] if recv[9] >= 0 else 0  # a source used twice
+    pol[5] = pol[9]
+    return recv, pol
+
+
+@pytest.mark.parametrize("window,delays", [(sfgb.SF_WINDOW_ALIGNED, [0, 5, -7, 64]),
+                                           (sfgb.SF_WINDOW_PACKET, None)])
+def test_stream_permutation_correlation_bit_exact(window, delays):
+    sh = orc.Shape(3, 4, 64, 36, 9, 4, 1)
+    rng = np.random.default_rng(17)
+    samples = rng.integers(-128, 128, size=sh.samples_shape(), dtype=np.int8)
+    scales = rng.integers(-1, 3, size=sh.scales_shape()).astype(np.int16)
+    recv, pol = _random_stream_perm(sh, 4)
+    plan = sfgb.Plan(sh.C, sh.F, sh.Tp, sh.R, sh.Rpp, sh.P, sh.B)
+    if delays is not None:
+        plan.set_subpacket_delays(delays)
+    plan.set_stream_permutation(recv, pol)
+    vis = torch.empty(plan.vis_shape(), dtype=torch.int32, device="cuda")
+    plan.correlate(_dev(samples, torch.int8), _dev(scales, torch.int16), window, vis)
+    torch.cuda.synchronize()
+    rc, bits = plan.status()
+    assert rc == 0 and bits == 0
+    got = vis.cpu().numpy()
+    # back to the identity: plain correlation again
+    plan.set_stream_permutation(None, None)
+    vis2 = torch.empty(plan.vis_shape(), dtype=torch.int32, device="cuda")
+    plan.correlate(_dev(samples, torch.int8), _dev(scales, torch.int16), window, vis2)
+    torch.cuda.synchronize()
+    plain = vis2.cpu().numpy()
+    plan.close()
+    off = orc.sample_offsets(sh, delays, mode="aligned" if window == sfgb.SF_WINDOW_ALIGNED else "packet")
+    re, im = orc.aligned_samples(sh, samples, scales, off)
+    pre, pim = orc.permute_streams(sh, re, im, recv, pol)
+    assert np.array_equal(got, orc.correlate(sh, pre, pim))
+    assert np.array_equal(plain, orc.correlate(sh, re, im))
+
+
+def test_stream_permutation_adaptive_chain_with_gains(lambda_cfg):
+    sh, samples, scales, weights, rfi = lambda_cfg
+    recv, pol = _random_stream_perm(sh, 8, n_zero=0)
+    rng = np.random.default_rng(23)
+    gains = (rng.uniform(0.5, 1.5, (sh.C, 2, sh.R)) * np.exp(1j * rng.uniform(0, 2 * np.pi, (sh.C, 2, sh.R))))
+    tau = rng.uniform(-5.0, 5.0, sh.R).astype(np.float32)
+    fixed = np.full(sh.C, 2)
+    plan = sfgb.Plan(sh.C, sh.F, sh.Tp, sh.R, sh.Rpp, sh.P, sh.B)
+    plan.set_weights(weights)
+    plan.set_fixed_counts(fixed)
+    plan.set_antenna_gains(gains)
+    plan.set_fine_delays(tau, 0.0, 781250.0, 64)
+    plan.set_stream_permutation(recv, pol)
+    s, sc = _dev(samples, torch.int8), _dev(scales, torch.int16)
+    vis = torch.empty(plan.vis_shape(), dtype=torch.int32, device="cuda")
+    cnt = torch.empty((sh.C, 2), dtype=torch.int32, device="cuda")
+    beams = torch.empty(plan.beams_shape(2), dtype=torch.float16, device="cuda")
+    plan.run_adaptive(s, sc, sfgb.SF_K_FIXED, 0.0, False, vis, None, None, cnt, beams)
+    torch.cuda.synchronize()
+    rc, bits = plan.status()
+    assert rc == 0 and bits == 0
+    plan.close()
+    ph = orc.fine_delay_phasors(sh, tau, 0.0, 781250.0, 64)
+    d = orc.permuted_factors(sh, recv, pol, gains=gains, phasors=ph)
+    ref = orc.adaptive_chain(sh, samples, scales, weights, k_fixed=fixed, d=d, perm=(recv, pol))
+    assert np.array_equal(vis.cpu().numpy(), ref["vis"])
+    yr = ref["beams"]
+    yb = beams.cpu().numpy().astype(np.float32)
+    yb = yb[..., 0] + 1j * yb[..., 1]
+    err = np.abs(yb - yr)
+    assert np.all(err[:, :, :sh.B] <= 2.0 ** -9 * np.abs(yr[:, :, :sh.B]) + 2.0 ** -6 +
+                  2e-3 * np.abs(yr[:, :, :sh.B]).max(axis=-1, keepdims=True))
+    assert np.all(err <= 2.0 ** -9 * np.abs(yr) + 2.0 ** -6 + 2e-3 * np.abs(yr).max(axis=-1, keepdims=True))
+
+
+def test_stream_permutation_rejects_bad_tables():
+    sh = orc.Shape(2, 4, 64, 36, 9, 2, 1)
+    plan = sfgb.Plan(sh.C, sh.F, sh.Tp, sh.R, sh.Rpp, sh.P, sh.B)
+    good_r = np.arange(2 * sh.R, dtype=np.int32) // 2
+    good_p = np.arange(2 * sh.R, dtype=np.int32) % 2
+    bad_r = good_r.copy()
+    bad_r[3] = sh.R
+    with pytest.raises(RuntimeError):
+        plan.set_stream_permutation(bad_r, good_p)
+    bad_p = good_p.copy()
+    bad_p[4] = 2
+    with pytest.raises(RuntimeError):
+        plan.set_stream_permutation(good_r, bad_p)
+    with pytest.raises(ValueError):
+        plan.set_stream_permutation(good_r[:-2], good_p[:-2])
+    pipe = sfgb.LambdaGPUPipeline((sh.C, sh.F, sh.Tp, sh.R, sh.Rpp, sh.P, sh.B), orc.synth_weights(sh))
+    with pytest.raises(RuntimeError):
+        pipe.set_stream_permutation(list(good_r[:-1]), list(good_p[:-1]))
+    pipe.set_stream_permutation(list(good_r), list(good_p))  # identity table is accepted
+    pipe.plan.close()
+    plan.close()
