@@ -65,7 +65,12 @@ BYTES_PER_UNIT = BYTES_IN + BYTES_VIS + 8 * B * 2 * T  # fp32-complex beam conve
 KERNEL_BYTES = {
     "sf_corr_kernel": BYTES_IN + BYTES_VIS,
     "sf_beam_kernel": BYTES_IN + BYTES_BEAMS_FP16,
+    # spectra tails: fp16 beams in, float spectra out
+    "sf_packet_spectra_kernel": BYTES_BEAMS_FP16 + 2 * 2 * B * (TP - 10) * 4,
+    "sf_beam_spectra_kernel": BYTES_BEAMS_FP16 + 2 * 2 * B * (T // 128) * 4,
 }
+MAIN_STAGES = ("sf_corr_kernel", "sf_eig_kernel", "sf_beam_kernel")
+TRIM, DOWNSAMPLE = 5, 128  # NR_FINE_CHANNELS_TO_REMOVE_EACH_SIDE; FFT_DOWNSAMPLE_FACTOR default
 
 
 def _set_channels(n):
@@ -91,7 +96,9 @@ def run_stage_only(args):
     cnt = torch.empty((C, 2), dtype=torch.int32, device="cuda")
     beams = torch.empty(plan.beams_shape(2), dtype=torch.float16, device="cuda")
     plan.correlate(d_s[0], d_sc[0], sfgb.SF_WINDOW_ALIGNED, vis, stream=stream)
-    name = {"corr": "sf_corr_kernel", "eig": "sf_eig_kernel", "beam": "sf_beam_kernel"}[args.only_stage]
+    name = {"corr": "sf_corr_kernel", "eig": "sf_eig_kernel", "beam": "sf_beam_kernel",
+            "packet_spectra": "sf_packet_spectra_kernel",
+            "beam_spectra": "sf_beam_spectra_kernel"}[args.only_stage]
     res = _stage_breakdown(plan, d_s, d_sc, vis, ev, cnt, beams, stream, args.steps, only=name)
     rc, bits = plan.status(stream)
     if rc != 0:
@@ -269,6 +276,7 @@ def run_ours(args, world, rank):
         raise RuntimeError(f"device status 0x{bits:x} after timing")
 
     hbm, tf, peak_kind = measured_peaks()
+    tail = {k: kernels.pop(k) for k in list(kernels) if k not in MAIN_STAGES}
     dom = max(kernels, key=lambda k: kernels[k]["ms"])
     dom_ms = kernels[dom]["ms"]
     if dom in KERNEL_BYTES:
@@ -294,6 +302,10 @@ def run_ours(args, world, rank):
         "config": dict(WORKLOAD, parallelism=f"channel shards x{world}" if world > 1 else "single GPU"),
         "roofline": roof,
         "kernels_ms": {k: round(v["ms"], 4) for k, v in kernels.items()},
+        # the reference's spectra tails on this step's 16 beams, timed alone (not in `value`)
+        "spectra_tail": {k: {"ms": round(v["ms"], 4),
+                             "GB/s": round(KERNEL_BYTES[k] * C / (v["ms"] / 1e3) / 1e9, 1)}
+                         for k, v in tail.items()},
         "e2e": e2e,
         "gpu_launches": 3 * args.steps,
         "clocks": clk,
@@ -324,7 +336,11 @@ def _stage_breakdown(plan, d_s, d_sc, vis, ev, cnt, beams, stream, reps, only=No
                                                        False, ev, None, cnt, None, stream=stream),
         "sf_beam_kernel": lambda i: plan.beamform(d_s[i % 2], d_sc[i % 2], sfgb.SF_WINDOW_ALIGNED, 2, beams,
                                                   stream=stream),
+        "sf_packet_spectra_kernel": lambda i: plan.packet_spectra(beams, 2 * B, TRIM, spec_pk, stream=stream),
+        "sf_beam_spectra_kernel": lambda i: plan.beam_spectra(beams, 2 * B, DOWNSAMPLE, spec_bs, stream=stream),
     }
+    spec_pk = torch.empty(plan.packet_spectra_shape(2 * B, TRIM), dtype=torch.float32, device=beams.device)
+    spec_bs = torch.empty(plan.beam_spectra_shape(2 * B, DOWNSAMPLE), dtype=torch.float32, device=beams.device)
     out = {}
     for name, fn in stages.items():
         if only is not None and name != only:
@@ -466,7 +482,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--channels", type=int, default=C,
                     help="channels per integration (default: the 384-channel workload)")
-    ap.add_argument("--only-stage", choices=["corr", "eig", "beam"],
+    ap.add_argument("--only-stage", choices=["corr", "eig", "beam", "packet_spectra", "beam_spectra"],
                     help="launch one stage kernel only (for a profiler capture)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

@@ -48,6 +48,7 @@ void free_plan(sf_plan *p) {
   cudaFree(p->d_perm);
   cudaFree(p->d_weights);
   cudaFree(p->d_weff);
+  cudaFree(p->d_spec_tw);
   cudaFree(p->d_fixed_counts);
   cudaFree(p->d_vis);
   cudaFree(p->d_evals);
@@ -173,6 +174,7 @@ int sf_plan_create(const sf_shape *shape, sf_plan **out_plan) {
   SF_ALLOC(p->d_evals, sizeof(float) * C * 4 * R);
   SF_ALLOC(p->d_counts, sizeof(int32_t) * C * 2);
   SF_ALLOC(p->d_status, sizeof(uint32_t));
+  if (sf_beam_spectra_supported(p->T)) SF_ALLOC(p->d_spec_tw, sizeof(float2) * p->T);
 #undef SF_ALLOC
   cudaError_t ez = cudaSuccess;
   ez = ez != cudaSuccess ? ez : cudaMemset(p->d_off_packet, 0, sizeof(int32_t) * p->F);
@@ -180,6 +182,7 @@ int sf_plan_create(const sf_shape *shape, sf_plan **out_plan) {
   ez = ez != cudaSuccess ? ez : cudaMemset(p->d_weff, 0, sizeof(float2) * C * 4 * B * R);
   ez = ez != cudaSuccess ? ez : cudaMemset(p->d_fixed_counts, 0, sizeof(int32_t) * C);
   ez = ez != cudaSuccess ? ez : cudaMemset(p->d_status, 0, sizeof(uint32_t));
+  if (p->d_spec_tw) ez = ez != cudaSuccess ? ez : sf_fill_spectra_twiddles(p->d_spec_tw, p->T);
   if (ez != cudaSuccess) {
     free_plan(p);
     return cuda_err(ez, "initialise plan memory");
@@ -379,6 +382,40 @@ int sf_beamform(sf_plan *plan, const int8_t *d_samples, const int16_t *d_scales,
   SF_TRY(sf_launch_beam(plan, d_samples, d_scales, off, n_slots,
                         reinterpret_cast<__half2 *>(d_beams_f16), s),
          "beam launch");
+  return SF_OK;
+}
+
+int sf_beam_spectra(sf_plan *plan, const uint16_t *d_beams_f16, int32_t n_beams_out,
+                    int32_t downsample, float *d_spectra, void *stream) {
+  if (int rc = check_plan(plan)) return rc;
+  if (!d_beams_f16 || !d_spectra) return set_err(SF_ERR_INVALID_ARGUMENT, "NULL buffer");
+  if (n_beams_out < 1) return set_err(SF_ERR_INVALID_ARGUMENT, "n_beams_out must be >= 1");
+  if (downsample < 1 || downsample > plan->T)
+    return set_err(SF_ERR_INVALID_ARGUMENT, "downsample %d outside [1, T = %d]", downsample, plan->T);
+  if (!plan->d_spec_tw)
+    return set_err(SF_ERR_UNSUPPORTED,
+                   "whole-integration spectra need T = P * Tp a power of two in [64, 16384] (T = %d)",
+                   plan->T);
+  SF_TRY(sf_launch_beam_spectra(plan, reinterpret_cast<const __half2 *>(d_beams_f16), n_beams_out,
+                                downsample, d_spectra, as_stream(stream)),
+         "beam spectra launch");
+  return SF_OK;
+}
+
+int sf_packet_spectra(sf_plan *plan, const uint16_t *d_beams_f16, int32_t n_beams_out, int32_t trim,
+                      float *d_spectra, void *stream) {
+  if (int rc = check_plan(plan)) return rc;
+  if (!d_beams_f16 || !d_spectra) return set_err(SF_ERR_INVALID_ARGUMENT, "NULL buffer");
+  if (n_beams_out < 1) return set_err(SF_ERR_INVALID_ARGUMENT, "n_beams_out must be >= 1");
+  if (reinterpret_cast<uintptr_t>(d_beams_f16) % 16 != 0)
+    return set_err(SF_ERR_INVALID_ARGUMENT, "beams must be 16-byte aligned");
+  if (!sf_packet_spectra_supported(plan->Tp))
+    return set_err(SF_ERR_UNSUPPORTED, "packet spectra need Tp in {16, 32, 64} (Tp = %d)", plan->Tp);
+  if (trim < 0 || 2 * trim >= plan->Tp)
+    return set_err(SF_ERR_INVALID_ARGUMENT, "trim %d outside [0, Tp/2)", trim);
+  SF_TRY(sf_launch_packet_spectra(plan, reinterpret_cast<const __half2 *>(d_beams_f16), n_beams_out,
+                                  trim, d_spectra, as_stream(stream)),
+         "packet spectra launch");
   return SF_OK;
 }
 

@@ -165,6 +165,20 @@ SF_DEVICE void cp_async_mbar_arrive(uint64_t *bar) {
   asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+// 16-byte asynchronous global -> shared copy (L2 only), tracked by commit
+// groups: cp_async_wait<N>() returns once at most N groups are still pending.
+SF_DEVICE void cp_async16(void *smem_dst, const void *gmem_src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem_dst)), "l"(gmem_src)
+               : "memory");
+}
+
+SF_DEVICE void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+template <int N>
+SF_DEVICE void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 // ---------------------------------------------------------------------------
 // tcgen05: tensor memory and the single-thread UMMA
 // ---------------------------------------------------------------------------

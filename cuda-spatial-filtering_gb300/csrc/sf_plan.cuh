@@ -35,6 +35,10 @@ struct sf_plan {
   int32_t *d_fixed_counts;  // [C]
   int32_t *h_fixed_counts;  // [C]
 
+  // W_T^k (k < T) for the whole-integration spectra; NULL when T is not a
+  // power of two in [64, 16384].
+  float2 *d_spec_tw;
+
   // Scratch for the whole-chain entry points.
   int32_t *d_vis;      // [C][NBL][2][2][2]
   float *d_evals;      // [C][2][2][R]
@@ -70,3 +74,12 @@ cudaError_t sf_launch_vis_accumulate(const sf_plan *p, const int32_t *vis, int64
                                      cudaStream_t stream);
 cudaError_t sf_launch_vis_to_float(const sf_plan *p, const int64_t *accum, float *out,
                                    cudaStream_t stream);
+
+// Beam spectra (sf_spectra.cu).
+int sf_beam_spectra_supported(int T);
+int sf_packet_spectra_supported(int Tp);
+cudaError_t sf_fill_spectra_twiddles(float2 *d_tw, int T);
+cudaError_t sf_launch_beam_spectra(const sf_plan *p, const __half2 *beams, int n_beams_out,
+                                   int downsample, float *out, cudaStream_t stream);
+cudaError_t sf_launch_packet_spectra(const sf_plan *p, const __half2 *beams, int n_beams_out,
+                                     int trim, float *out, cudaStream_t stream);

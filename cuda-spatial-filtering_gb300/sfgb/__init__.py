@@ -66,6 +66,8 @@ _SIGS = {
     "sf_beamform": ([_P, _P, _P, _I32, _I32, _P, _P], ctypes.c_int),
     "sf_accumulate_visibilities": ([_P, _P, _P, _P], ctypes.c_int),
     "sf_visibilities_to_float": ([_P, _P, _P, _P], ctypes.c_int),
+    "sf_beam_spectra": ([_P, _P, _I32, _I32, _P, _P], ctypes.c_int),
+    "sf_packet_spectra": ([_P, _P, _I32, _I32, _P, _P], ctypes.c_int),
     "sf_run_corr_beam": ([_P, _P, _P, _P, _P, _P], ctypes.c_int),
     "sf_run_lambda_gpu": ([_P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "sf_run_adaptive": ([_P, _P, _P, _I32, ctypes.c_float, _I32, _P, _P, _P, _P, _P, _P], ctypes.c_int),
@@ -232,6 +234,22 @@ class Plan:
 
     def visibilities_to_float(self, accum, out, stream=None):
         _check(lib().sf_visibilities_to_float(self._h, _ptr(accum), _ptr(out), _stream(stream)))
+
+    def beam_spectra(self, beams, n_beams_out, downsample, spectra, stream=None):
+        """Whole-integration |FFT|^2 spectra, downsampled by `downsample` bins."""
+        _check(lib().sf_beam_spectra(self._h, _ptr(beams), int(n_beams_out), int(downsample),
+                                     _ptr(spectra), _stream(stream)))
+
+    def packet_spectra(self, beams, n_beams_out, trim, spectra, stream=None):
+        """Per-packet |FFT| summed over packets, `trim` edge bins dropped each side."""
+        _check(lib().sf_packet_spectra(self._h, _ptr(beams), int(n_beams_out), int(trim),
+                                       _ptr(spectra), _stream(stream)))
+
+    def beam_spectra_shape(self, n_beams_out, downsample):
+        return (self.C, 2, n_beams_out, self.T // downsample)
+
+    def packet_spectra_shape(self, n_beams_out, trim):
+        return (self.C, 2, n_beams_out, self.Tp - 2 * trim)
 
     # ---- whole chains ----
     def run_corr_beam(self, samples, scales, vis, beams, stream=None):

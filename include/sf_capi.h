@@ -16,6 +16,7 @@
  *   evals    float  [batch][R] ascending;  evecs float2 [batch][R(k)][R(l)] (component l of
  *                                                        eigenvector k)
  *   beams    fp16   [C][Pol][NB][T][2]                  (LambdaConfig::BeamOutputType)
+ *   spectra  float  [C][Pol][NB][bins]                  (FFTOutputType of each pipeline)
  * where R = F * Rpp receivers, T = P * Tp samples per integration.
  *
  * Every entry point is asynchronous on the given stream, never synchronises
@@ -172,6 +173,28 @@ int sf_accumulate_visibilities(sf_plan *plan, const int32_t *d_vis, int64_t *d_a
                                void *stream);
 int sf_visibilities_to_float(sf_plan *plan, const int64_t *d_accum, float *d_vis_f32,
                              void *stream);
+
+/* ---- beam spectra ------------------------------------------------------------ */
+
+/* LambdaGPUPipeline's spectra tail (reference lambda_gpu_pipeline.hpp:522-531 with the cuFFT plan
+ * of :814-817/:944-947, detect_and_downsample_fft spatial.cuh:795-848): per (channel, pol, beam)
+ * a forward T-point FFT of the beam series (X[k] = sum_n x[n] exp(-2 pi i n k / T), fp32), then
+ * bin g = mean of |X|^2 over bins g D .. g D + D - 1 with NaN bins skipped (0 if all NaN).
+ *   d_beams_f16  fp16 pairs [C][Pol][n_beams_out][T][2] (sf_beamform's output)
+ *   d_spectra    float [C][Pol][n_beams_out][T / downsample]  (FFTOutputType)
+ * T = P * Tp must be a power of two in [64, 16384] (else SF_ERR_UNSUPPORTED). */
+int sf_beam_spectra(sf_plan *plan, const uint16_t *d_beams_f16, int32_t n_beams_out,
+                    int32_t downsample, float *d_spectra, void *stream);
+
+/* The adaptive pipeline's spectra tail (reference lambda_adaptive_beamformed_spectra_pipeline.hpp:
+ * 808-848, sum_fft_over_packets spatial.cuh:1508-1567): per (channel, pol, beam) and packet a
+ * Tp-point forward FFT, bins kept in the order Tp/2+trim .. Tp-1, 0 .. Tp/2-trim-1 (the reference
+ * uses trim = 5, NR_FINE_CHANNELS_TO_REMOVE_EACH_SIDE), |X| summed over the P packets.
+ *   d_beams_f16  fp16 pairs [C][Pol][n_beams_out][T][2], 16-byte aligned
+ *   d_spectra    float [C][Pol][n_beams_out][Tp - 2 trim]
+ * Tp must be 16, 32 or 64 (the reference's plan is fixed at 64). */
+int sf_packet_spectra(sf_plan *plan, const uint16_t *d_beams_f16, int32_t n_beams_out, int32_t trim,
+                      float *d_spectra, void *stream);
 
 /* ---- whole chains (what the drop-in pipelines run per buffer) -------------- */
 

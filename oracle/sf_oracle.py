@@ -401,6 +401,72 @@ def half_output(y):
 
 
 # --------------------------------------------------------------------------
+# Beam spectra tail
+# --------------------------------------------------------------------------
+# The reference transforms its beams with cuFFT (CUDA toolkit library, not part
+# of the reference tree): cufftXtMakePlanMany(1-D, C2C, fp32) executed with
+# CUFFT_FORWARD, i.e. the unnormalised DFT X[k] = sum_n x[n] exp(-2 pi i n k / N).
+# numpy.fft.fft computes the same definition; dft_direct below pins that by the
+# O(N^2) sum.
+def dft_direct(x):
+    """Forward DFT along the last axis by the definition (small N only)."""
+    x = np.asarray(x, dtype=np.complex128)
+    n = x.shape[-1]
+    k = np.arange(n)
+    w = np.exp(-2j * np.pi * np.outer(k, k) / n)
+    return x @ w.T
+
+
+def beams_from_half(beams_f16):
+    """fp16 pairs [..., T, 2] -> complex128 [..., T]."""
+    b = np.asarray(beams_f16).astype(np.float64)
+    return b[..., 0] + 1j * b[..., 1]
+
+
+def beam_spectra(beams_c, downsample):
+    """LambdaGPUPipeline spectra tail: one forward FFT of each (channel, pol,
+    beam) series over the whole integration (lambda_gpu_pipeline.hpp:522-524;
+    plan of length T = P Tp with C Pol B batches, :814-817 and :944-947), then
+    detect_and_downsample_fft (spatial.cuh:795-848): output bin g is the mean of
+    |X|^2 over bins g D .. g D + D - 1, NaN bins skipped, 0 when every bin of the
+    group is NaN; T // D bins ([C][Pol][B][T/D] floats)."""
+    beams_c = np.asarray(beams_c, dtype=np.complex128)
+    T = beams_c.shape[-1]
+    n_out = T // downsample
+    with np.errstate(invalid="ignore", over="ignore"):
+        x = np.fft.fft(beams_c, axis=-1)
+        pw = x.real * x.real + x.imag * x.imag
+    pw = pw[..., : n_out * downsample].reshape(beams_c.shape[:-1] + (n_out, downsample))
+    ok = ~np.isnan(pw)
+    s = np.where(ok, pw, 0.0).sum(axis=-1)
+    cnt = ok.sum(axis=-1)
+    return np.where(cnt > 0, s / np.maximum(cnt, 1), 0.0)
+
+
+def fine_channel_order(Tp, trim):
+    """FFT bins kept by the adaptive tail, in output order: the upper half
+    without its first `trim` bins, then the lower half without its last `trim`
+    (the two half-copies of lambda_adaptive_beamformed_spectra_pipeline.hpp:821-833
+    over the frequency-major tensor of :816-819)."""
+    return np.concatenate([np.arange(Tp // 2 + trim, Tp), np.arange(0, Tp // 2 - trim)])
+
+
+def packet_spectra(beams_c, Tp, trim):
+    """Adaptive pipeline spectra tail
+    (lambda_adaptive_beamformed_spectra_pipeline.hpp:808-848): a Tp-point FFT of
+    each packet of each (channel, pol, beam) series (plan :1046-1050, batch
+    2B C Pol P), the fine-channel trim/reorder, then sum_fft_over_packets
+    (spatial.cuh:1508-1567): sum over the P packets of the magnitude |X|
+    ([C][Pol][NB][Tp - 2 trim] floats)."""
+    beams_c = np.asarray(beams_c, dtype=np.complex128)
+    T = beams_c.shape[-1]
+    P = T // Tp
+    x = np.fft.fft(beams_c.reshape(beams_c.shape[:-1] + (P, Tp)), axis=-1)
+    mag = np.abs(x)[..., fine_channel_order(Tp, trim)]
+    return mag.sum(axis=-2)
+
+
+# --------------------------------------------------------------------------
 # Whole chains
 # --------------------------------------------------------------------------
 def corr_beam_chain(shape, samples, scales, weights, d=None, offsets=None):
