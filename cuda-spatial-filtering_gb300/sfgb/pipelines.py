@@ -9,14 +9,18 @@ targets:
   LambdaGPUPipeline               lambda_gpu_pipeline.hpp:445-608
   LambdaAdaptiveBeamformedSpectraPipeline
                                   lambda_adaptive_beamformed_spectra_pipeline.hpp:563-957
-                                  (projection, weights and beams; its FFT tail is
-                                  not part of this path)
 
 ``execute_pipeline`` takes a ``PacketData`` (the FinalPacketData payload:
 host samples/scales in the packet layout), copies it to the device, runs the
 chain, accumulates visibilities and lands the beams (and eigen outputs) in
 the ``Output`` object, as the reference does with cudaMemcpyAsync into
-landing pointers.  ``dump_visibilities`` converts the accumulator to the
+landing pointers.  LambdaGPUPipeline and the adaptive pipeline also land their
+spectra tails (``fft_output``): whole-integration |FFT|^2 downsampled by
+``fft_downsample_factor`` (lambda_gpu_pipeline.hpp:522-531), and per-packet |FFT|
+summed over packets with 5 edge bins trimmed each side
+(lambda_adaptive_beamformed_spectra_pipeline.hpp:808-848); shapes the spectra
+kernels do not cover (T not a power of two in [64, 16384]; Tp not 16, 32 or
+64) skip the tail and leave ``fft_output`` None.  ``dump_visibilities`` converts the accumulator to the
 reference's float layout and resets it.
 """
 from __future__ import annotations
@@ -54,13 +58,19 @@ class SingleHostMemoryOutput:
         self.eigenvalues = None
         self.eigenvectors = None
         self.nulled_eigenmode_counts = None
+        self.fft_output = None
         self.blocks = 0
+        self.fft_blocks = 0
 
     def register_beam_data_block(self, start_seq, end_seq):
         self.blocks += 1
         return 1
 
     def register_visibilities_block(self, start_seq, end_seq, missing, total):
+        return 1
+
+    def register_fft_block(self, start_seq, end_seq):
+        self.fft_blocks += 1
         return 1
 
 
@@ -127,7 +137,7 @@ class _Base(GPUPipeline):
             self.d_samples.copy_(s.reshape(self.d_samples.shape), non_blocking=False)
             self.d_scales.copy_(sc.reshape(self.d_scales.shape), non_blocking=False)
 
-    def _finish(self, packet_data, dummy_run, extra):
+    def _finish(self, packet_data, dummy_run, extra, spectra=None):
         import torch
         self.plan.accumulate_visibilities(self.d_vis, self.d_accum, stream=self.stream)
         if self.output_ is not None and not dummy_run:
@@ -136,6 +146,10 @@ class _Base(GPUPipeline):
                 self.output_.beam_data = self.d_beams.cpu().numpy()
                 for k, v in extra.items():
                     setattr(self.output_, k, v.cpu().numpy())
+            if spectra is not None:
+                self.output_.register_fft_block(packet_data.start_seq_id, packet_data.end_seq_id)
+                with torch.cuda.stream(self.stream):
+                    self.output_.fft_output = spectra.cpu().numpy()
             self.integrated += 1
             if self.integrated >= self.nr_blocks:
                 self.dump_visibilities()
@@ -161,19 +175,39 @@ class LambdaCorrBeamOnlyGPUPipeline(_Base):
         self._finish(packet_data, dummy_run, {})
 
 
+def whole_spectra_supported(T):
+    return 64 <= T <= 16384 and (T & (T - 1)) == 0
+
+
+def packet_spectra_supported(Tp):
+    return Tp in (16, 32, 64)
+
+
+FINE_CHANNELS_TO_REMOVE_EACH_SIDE = 5  # lambda_adaptive_beamformed_spectra_pipeline.hpp:23
+
+
 class LambdaGPUPipeline(_Base):
-    def __init__(self, shape, weights, nr_blocks_to_accumulate=1 << 30):
+    def __init__(self, shape, weights, nr_blocks_to_accumulate=1 << 30, fft_downsample_factor=128):
         import torch
         super().__init__(shape, weights, nr_blocks_to_accumulate)
         p = self.plan
         self.d_evals = torch.empty((p.C, 2, 2, p.R), dtype=torch.float32, device="cuda")
         self.d_evecs = torch.empty((p.C, 2, 2, p.R, p.R, 2), dtype=torch.float32, device="cuda")
+        self.fft_downsample = int(fft_downsample_factor)
+        self.d_spectra = None
+        if whole_spectra_supported(p.T) and 1 <= self.fft_downsample <= p.T:
+            self.d_spectra = torch.empty(p.beam_spectra_shape(p.B, self.fft_downsample), dtype=torch.float32,
+                                         device="cuda")
 
     def execute_pipeline(self, packet_data, dummy_run=False):
         self._ingest(packet_data)
         self.plan.run_lambda_gpu(self.d_samples, self.d_scales, self.d_vis, self.d_evals, self.d_evecs,
                                  self.d_beams, stream=self.stream)
-        self._finish(packet_data, dummy_run, {"eigenvalues": self.d_evals, "eigenvectors": self.d_evecs})
+        if self.d_spectra is not None:
+            self.plan.beam_spectra(self.d_beams, self.plan.B, self.fft_downsample, self.d_spectra,
+                                   stream=self.stream)
+        self._finish(packet_data, dummy_run, {"eigenvalues": self.d_evals, "eigenvectors": self.d_evecs},
+                     spectra=self.d_spectra)
 
 
 class LambdaAdaptiveBeamformedSpectraPipeline(_Base):
@@ -195,11 +229,19 @@ class LambdaAdaptiveBeamformedSpectraPipeline(_Base):
         self.d_evals = torch.empty((p.C, 2, p.R), dtype=torch.float32, device="cuda")
         self.d_evecs = torch.empty((p.C, 2, p.R, p.R, 2), dtype=torch.float32, device="cuda")
         self.d_counts = torch.empty((p.C, 2), dtype=torch.int32, device="cuda")
+        self.d_spectra = None
+        if packet_spectra_supported(p.Tp):
+            self.d_spectra = torch.empty(p.packet_spectra_shape(2 * p.B, FINE_CHANNELS_TO_REMOVE_EACH_SIDE),
+                                         dtype=torch.float32, device="cuda")
 
     def execute_pipeline(self, packet_data, dummy_run=False):
         self._ingest(packet_data)
         self.plan.run_adaptive(self.d_samples, self.d_scales, self.k_rule, self.delta, self.shrink,
                                self.d_vis, self.d_evals, self.d_evecs, self.d_counts, self.d_beams,
                                stream=self.stream)
+        if self.d_spectra is not None:
+            self.plan.packet_spectra(self.d_beams, 2 * self.plan.B, FINE_CHANNELS_TO_REMOVE_EACH_SIDE,
+                                     self.d_spectra, stream=self.stream)
         self._finish(packet_data, dummy_run, {"eigenvalues": self.d_evals, "eigenvectors": self.d_evecs,
-                                              "nulled_eigenmode_counts": self.d_counts})
+                                              "nulled_eigenmode_counts": self.d_counts},
+                     spectra=self.d_spectra)

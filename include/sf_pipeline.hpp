@@ -37,8 +37,18 @@
  * visibilities, lands beams (and eigen outputs) in the Output's landing
  * pointers with transfer-complete callbacks, and dumps the visibilities every
  * nr_blocks_to_accumulate runs.  Errors throw std::runtime_error carrying
- * sf_last_error() (the reference exits through CUDA_CHECK).  Beam steering
- * and the spectra FFT tail are not part of this path.
+ * sf_last_error() (the reference exits through CUDA_CHECK).
+ *
+ * Spectra tails: SfLambdaGPUPipeline lands |FFT|^2 of each beam over the whole
+ * integration downsampled by Config::FFT_DOWNSAMPLE_FACTOR (128 when Config has
+ * none; float [C][Pol][B][T/D], lambda_gpu_pipeline.hpp:522-531, 585-595), and
+ * SfLambdaAdaptivePipeline lands the per-packet |FFT| summed over packets with
+ * 5 bins trimmed each side (float [C][Pol][2B][Tp-10],
+ * lambda_adaptive_beamformed_spectra_pipeline.hpp:808-848, 899-911), through
+ * Output::register_fft_block / get_fft_landing_pointer /
+ * register_fft_transfer_complete.  Shapes the spectra kernels do not cover
+ * (T not a power of two in [64, 16384]; Tp not 16, 32 or 64) skip the tail and
+ * register no FFT block.  Beam steering is not part of this path.
  */
 #ifndef SF_PIPELINE_HPP
 #define SF_PIPELINE_HPP
@@ -52,6 +62,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <unordered_map>
 #include <vector>
 
@@ -96,15 +107,27 @@ template <typename State> void release_buffer_cb(void *data) {
 template <typename Out> struct TransferContext {
   std::shared_ptr<Out> output;
   size_t block;
-  int kind;  // 0 beams, 1 visibilities, 2 eigendecomposition
+  int kind;  // 0 beams, 1 visibilities, 2 eigendecomposition, 3 spectra
 };
 template <typename Out> void transfer_complete_cb(void *data) {
   auto *ctx = static_cast<TransferContext<Out> *>(data);
   if (ctx->kind == 0) ctx->output->register_beam_data_transfer_complete(ctx->block);
   else if (ctx->kind == 1) ctx->output->register_visibilities_transfer_complete(ctx->block);
-  else ctx->output->register_eigendecomposition_data_transfer_complete(ctx->block);
+  else if (ctx->kind == 2) ctx->output->register_eigendecomposition_data_transfer_complete(ctx->block);
+  else ctx->output->register_fft_transfer_complete(ctx->block);
   delete ctx;
 }
+
+// Config::FFT_DOWNSAMPLE_FACTOR, or LambdaConfig's default of 128.
+template <typename Cfg, typename = void> struct FftDownsample {
+  static constexpr int value = 128;
+};
+template <typename Cfg>
+struct FftDownsample<Cfg, std::void_t<decltype(Cfg::FFT_DOWNSAMPLE_FACTOR)>> {
+  static constexpr int value = static_cast<int>(Cfg::FFT_DOWNSAMPLE_FACTOR);
+};
+
+constexpr bool pow2_in(int n, int lo, int hi) { return n >= lo && n <= hi && (n & (n - 1)) == 0; }
 
 }  // namespace detail
 
@@ -124,6 +147,13 @@ template <typename Config, typename Base, int Mode> class SfPipelineBase : publi
   static constexpr int T = P * TP;
   static constexpr int NBL = R * (R + 1) / 2;
   static constexpr int SLOTS = Mode == kAdaptive ? 2 : 1;  // adaptive: original + projected beams
+  // Spectra tails (see the file comment): bins per (channel, pol, beam) row.
+  static constexpr int FFT_TRIM = 5;  // NR_FINE_CHANNELS_TO_REMOVE_EACH_SIDE
+  static constexpr int FFT_DOWNSAMPLE = detail::FftDownsample<Config>::value;
+  static constexpr bool SPECTRA =
+      (Mode == kLambdaGpu && detail::pow2_in(T, 64, 16384) && FFT_DOWNSAMPLE >= 1 && FFT_DOWNSAMPLE <= T) ||
+      (Mode == kAdaptive && detail::pow2_in(TP, 16, 64));
+  static constexpr int FFT_BINS = Mode == kAdaptive ? TP - 2 * FFT_TRIM : T / (FFT_DOWNSAMPLE > 0 ? FFT_DOWNSAMPLE : 1);
   static_assert(POL == 2, "the GB300 path handles two polarisations");
   static_assert(F * RPP == R, "NR_RECEIVERS must equal NR_FPGA_SOURCES x NR_RECEIVERS_PER_PACKET");
 
@@ -154,6 +184,7 @@ template <typename Config, typename Base, int Mode> class SfPipelineBase : publi
         b->evals.allocate((size_t)C * POL * R);
         b->counts.allocate((size_t)C * POL);
       }
+      if (SPECTRA) b->spectra.allocate((size_t)C * POL * SLOTS * B * FFT_BINS);
       detail::check(sf_set_weights(b->plan, reinterpret_cast<const uint16_t *>(h_weights), b->stream),
                     "sf_set_weights");
     }
@@ -242,6 +273,7 @@ template <typename Config, typename Base, int Mode> class SfPipelineBase : publi
     }
 
     run_chain(b);
+    if (SPECTRA) run_spectra(b);
 
     // integrate: accumulations of successive buffers are chained in order
     detail::check_cuda(cudaStreamWaitEvent(b.stream, last_accumulate_, 0), "cudaStreamWaitEvent");
@@ -308,9 +340,30 @@ template <typename Config, typename Base, int Mode> class SfPipelineBase : publi
     detail::DeviceArray<uint16_t> beams;
     detail::DeviceArray<float> evals, evecs;
     detail::DeviceArray<int32_t> counts;
+    detail::DeviceArray<float> spectra;
   };
 
   virtual void run_chain(Buffer &b) = 0;
+
+  void run_spectra(Buffer &b) {
+    if (Mode == kAdaptive)
+      detail::check(sf_packet_spectra(b.plan, b.beams.ptr, SLOTS * B, FFT_TRIM, b.spectra.ptr, b.stream),
+                    "sf_packet_spectra");
+    else
+      detail::check(sf_beam_spectra(b.plan, b.beams.ptr, SLOTS * B, FFT_DOWNSAMPLE, b.spectra.ptr, b.stream),
+                    "sf_beam_spectra");
+  }
+
+  void land_spectra(Buffer &b, size_t start_seq, size_t end_seq) {
+    if (!SPECTRA) return;
+    Output &out = *this->output_;
+    const size_t block = out.register_fft_block(start_seq, end_seq);
+    if (block == std::numeric_limits<size_t>::max()) return;
+    detail::check_cuda(cudaMemcpyAsync(out.get_fft_landing_pointer(block), b.spectra.ptr, b.spectra.bytes(),
+                                       cudaMemcpyDefault, b.stream),
+                       "cudaMemcpyAsync");
+    launch_transfer_done(b.stream, block, 3);
+  }
 
   void launch_transfer_done(cudaStream_t s, size_t block, int kind) {
     auto *ctx = new detail::TransferContext<Output>{this->output_, block, kind};
@@ -330,6 +383,13 @@ template <typename Config, typename Base, int Mode> class SfPipelineBase : publi
       out.register_arrivals_transfer_complete(block);
     }
     if (Mode == kCorrBeam) return;
+    if (Mode == kAdaptive) land_spectra(b, start_seq, end_seq);  // beams, spectra, eigen (reference order)
+    land_eigen(b, start_seq, end_seq);
+    if (Mode == kLambdaGpu) land_spectra(b, start_seq, end_seq);  // beams, eigen, spectra
+  }
+
+  void land_eigen(Buffer &b, size_t start_seq, size_t end_seq) {
+    Output &out = *this->output_;
     const size_t eblock = out.register_eigendecomposition_data_block(start_seq, end_seq);
     if (eblock == std::numeric_limits<size_t>::max()) return;
     detail::check_cuda(cudaMemcpyAsync(out.get_eigenvalues_data_landing_pointer(eblock), b.evals.ptr,

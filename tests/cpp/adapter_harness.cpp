@@ -11,7 +11,7 @@
 //   reads  dir/samples.bin (int8, two integrations), dir/scales.bin (int16, two),
 //          dir/weights.bin (fp16 pairs)
 //   writes dir/beams_<run>.bin, dir/vis.bin (float, after one dump of both runs),
-//          dir/evals_<run>.bin, dir/counts_<run>.bin, dir/protocol.txt
+//          dir/evals_<run>.bin, dir/counts_<run>.bin, dir/fft_<run>.bin, dir/protocol.txt
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -43,16 +43,19 @@ class Output {
   virtual size_t register_visibilities_block(const size_t start_seq_num, const size_t end_seq_num,
                                              const int num_missing_packets, const int num_total_packets) = 0;
   virtual size_t register_eigendecomposition_data_block(const size_t start_seq_num, const size_t end_seq_num) = 0;
+  virtual size_t register_fft_block(const size_t start_seq_num, const size_t end_seq_num) = 0;
   virtual void *get_beam_data_landing_pointer(const size_t block_num) = 0;
   virtual void *get_visibilities_landing_pointer(const size_t block_num) = 0;
   virtual void *get_arrivals_data_landing_pointer(const size_t block_num) = 0;
   virtual void *get_eigenvalues_data_landing_pointer(const size_t block_num) = 0;
   virtual void *get_eigenvectors_data_landing_pointer(const size_t block_num) = 0;
   virtual void *get_nulled_eigenmode_counts_landing_pointer(const size_t block_num) = 0;
+  virtual void *get_fft_landing_pointer(const size_t block_num) = 0;
   virtual void register_beam_data_transfer_complete(const size_t block_num) = 0;
   virtual void register_visibilities_transfer_complete(const size_t block_num) = 0;
   virtual void register_arrivals_transfer_complete(const size_t block_num) = 0;
   virtual void register_eigendecomposition_data_transfer_complete(const size_t block_num) = 0;
+  virtual void register_fft_transfer_complete(const size_t block_num) = 0;
 };
 
 struct FinalPacketData {
@@ -102,6 +105,7 @@ struct TestConfig {
   static constexpr int NR_POLARIZATIONS = 2;
   static constexpr int NR_PACKETS_FOR_CORRELATION = 8;
   static constexpr int NR_BEAMS = 3;
+  static constexpr int FFT_DOWNSAMPLE_FACTOR = 16;
 };
 using Cfg = TestConfig;
 constexpr size_t kSamples = (size_t)Cfg::NR_CHANNELS * (Cfg::NR_PACKETS_FOR_CORRELATION + 2) *
@@ -151,19 +155,29 @@ class RecordingState : public ProcessorStateBase {
 class HostOutput : public Output {
  public:
   static constexpr size_t kBlocks = 4;
-  std::vector<std::vector<char>> beams, vis, evals, evecs, counts, arrivals;
-  std::atomic<int> beam_done{0}, vis_done{0}, eig_done{0}, arrivals_done{0};
-  size_t next_beam = 0, next_eig = 0;
+  std::vector<std::vector<char>> beams, vis, evals, evecs, counts, arrivals, fft;
+  std::atomic<int> beam_done{0}, vis_done{0}, eig_done{0}, arrivals_done{0}, fft_done{0};
+  size_t next_beam = 0, next_eig = 0, next_fft = 0;
+  std::vector<std::string> order;  // block registrations in call order
   int vis_missing = -1, vis_total = -1;
   uint64_t vis_start = 0, vis_end = 0;
-  HostOutput(size_t beam_bytes, size_t vis_bytes, size_t eval_bytes, size_t evec_bytes, size_t count_bytes)
+  HostOutput(size_t beam_bytes, size_t vis_bytes, size_t eval_bytes, size_t evec_bytes, size_t count_bytes,
+             size_t fft_bytes)
       : beams(kBlocks, std::vector<char>(beam_bytes)),
         vis(1, std::vector<char>(vis_bytes)),
         evals(kBlocks, std::vector<char>(eval_bytes)),
         evecs(kBlocks, std::vector<char>(evec_bytes)),
         counts(kBlocks, std::vector<char>(count_bytes)),
-        arrivals(kBlocks, std::vector<char>(kArrivals)) {}
-  size_t register_beam_data_block(const size_t, const size_t) override { return next_beam++ % kBlocks; }
+        arrivals(kBlocks, std::vector<char>(kArrivals)),
+        fft(kBlocks, std::vector<char>(fft_bytes)) {}
+  size_t register_beam_data_block(const size_t, const size_t) override {
+    order.push_back("beam");
+    return next_beam++ % kBlocks;
+  }
+  size_t register_fft_block(const size_t, const size_t) override {
+    order.push_back("fft");
+    return next_fft++ % kBlocks;
+  }
   size_t register_visibilities_block(const size_t s, const size_t e, const int missing, const int total) override {
     vis_start = s;
     vis_end = e;
@@ -171,17 +185,22 @@ class HostOutput : public Output {
     vis_total = total;
     return 0;
   }
-  size_t register_eigendecomposition_data_block(const size_t, const size_t) override { return next_eig++ % kBlocks; }
+  size_t register_eigendecomposition_data_block(const size_t, const size_t) override {
+    order.push_back("eig");
+    return next_eig++ % kBlocks;
+  }
   void *get_beam_data_landing_pointer(const size_t b) override { return beams[b].data(); }
   void *get_visibilities_landing_pointer(const size_t) override { return vis[0].data(); }
   void *get_arrivals_data_landing_pointer(const size_t b) override { return arrivals[b].data(); }
   void *get_eigenvalues_data_landing_pointer(const size_t b) override { return evals[b].data(); }
   void *get_eigenvectors_data_landing_pointer(const size_t b) override { return evecs[b].data(); }
   void *get_nulled_eigenmode_counts_landing_pointer(const size_t b) override { return counts[b].data(); }
+  void *get_fft_landing_pointer(const size_t b) override { return fft[b].data(); }
   void register_beam_data_transfer_complete(const size_t) override { ++beam_done; }
   void register_visibilities_transfer_complete(const size_t) override { ++vis_done; }
   void register_arrivals_transfer_complete(const size_t) override { ++arrivals_done; }
   void register_eigendecomposition_data_transfer_complete(const size_t) override { ++eig_done; }
+  void register_fft_transfer_complete(const size_t) override { ++fft_done; }
 };
 
 static std::vector<char> read_file(const std::string &path, size_t bytes) {
@@ -218,7 +237,10 @@ int main(int argc, char **argv) {
     const size_t eval_bytes = mode == 1 ? (size_t)C * 4 * R * 4 : (size_t)C * 2 * R * 4;
     const size_t evec_bytes = mode == 1 ? (size_t)C * 4 * R * R * 8 : 8;
     const size_t count_bytes = (size_t)C * 2 * 4;
-    auto output = std::make_shared<HostOutput>(beam_bytes, vis_bytes, eval_bytes, evec_bytes, count_bytes);
+    const size_t fft_bytes = mode == 2 ? (size_t)C * 2 * 2 * B * (Cfg::NR_TIME_STEPS_PER_PACKET - 10) * 4
+                                       : (size_t)C * 2 * B * (T / Cfg::FFT_DOWNSAMPLE_FACTOR) * 4;
+    auto output =
+        std::make_shared<HostOutput>(beam_bytes, vis_bytes, eval_bytes, evec_bytes, count_bytes, fft_bytes);
     RecordingState state;
 
     std::unique_ptr<GPUPipeline> pipeline;
@@ -257,6 +279,7 @@ int main(int argc, char **argv) {
       write_file(dir + "/beams_" + std::to_string(run) + ".bin", output->beams[run].data(), beam_bytes);
       write_file(dir + "/evals_" + std::to_string(run) + ".bin", output->evals[run].data(), eval_bytes);
       write_file(dir + "/counts_" + std::to_string(run) + ".bin", output->counts[run].data(), count_bytes);
+      write_file(dir + "/fft_" + std::to_string(run) + ".bin", output->fft[run].data(), fft_bytes);
     }
     write_file(dir + "/vis.bin", output->vis[0].data(), vis_bytes);
     std::ofstream proto(dir + "/protocol.txt");
@@ -265,7 +288,10 @@ int main(int argc, char **argv) {
     proto << "\nbeam_done " << output->beam_done << "\nvis_done " << output->vis_done << "\neig_done "
           << output->eig_done << "\narrivals_done " << output->arrivals_done << "\nvis_missing "
           << output->vis_missing << "\nvis_total " << output->vis_total << "\nvis_start " << output->vis_start
-          << "\nvis_end " << output->vis_end << "\nstatus " << bits << "\n";
+          << "\nvis_end " << output->vis_end << "\nfft_done " << output->fft_done << "\nstatus " << bits << "\n";
+    proto << "order";
+    for (const auto &o : output->order) proto << " " << o;
+    proto << "\n";
   } catch (const std::exception &e) {
     std::fprintf(stderr, "error: %s\n", e.what());
     return 1;

@@ -22,6 +22,7 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 # TestConfig of the harness
 C, F, TP, R, RPP, P, B = 6, 2, 16, 10, 5, 8, 3
+FFT_DOWNSAMPLE, FFT_TRIM = 16, 5
 DELAYS = [3, -5]
 K_MAP = [c % 3 for c in range(C)]
 
@@ -56,7 +57,7 @@ def _run(harness, mode, inputs, tmp_path):
     proto = {}
     for line in (tmp_path / "protocol.txt").read_text().splitlines():
         k, *v = line.split()
-        proto[k] = [int(x) for x in v]
+        proto[k] = v if k == "order" else [int(x) for x in v]
     return proto
 
 
@@ -75,7 +76,7 @@ def _direct(mode, inputs):
         plan.set_fixed_counts(np.array(K_MAP, np.int32))
     slots = 2 if mode == 2 else 1
     accum = torch.zeros(plan.vis_shape(), dtype=torch.int64, device="cuda")
-    out = {"beams": [], "evals": [], "counts": []}
+    out = {"beams": [], "evals": [], "counts": [], "fft": []}
     for run in range(2):
         s, sc = _dev(samples[run], torch.int8), _dev(scales[run], torch.int16)
         vis = torch.empty(plan.vis_shape(), dtype=torch.int32, device="cuda")
@@ -95,6 +96,14 @@ def _direct(mode, inputs):
             out["counts"].append(cnt.cpu().numpy())
         plan.accumulate_visibilities(vis, accum)
         out["beams"].append(beams.cpu().numpy())
+        if mode == 1:
+            spec = torch.empty(plan.beam_spectra_shape(B, FFT_DOWNSAMPLE), dtype=torch.float32, device="cuda")
+            plan.beam_spectra(beams, B, FFT_DOWNSAMPLE, spec)
+            out["fft"].append(spec.cpu().numpy())
+        elif mode == 2:
+            spec = torch.empty(plan.packet_spectra_shape(2 * B, FFT_TRIM), dtype=torch.float32, device="cuda")
+            plan.packet_spectra(beams, 2 * B, FFT_TRIM, spec)
+            out["fft"].append(spec.cpu().numpy())
     vis_f = torch.empty(plan.vis_shape(), dtype=torch.float32, device="cuda")
     plan.visibilities_to_float(accum, vis_f)
     out["vis"] = vis_f.cpu().numpy()
@@ -115,6 +124,9 @@ def test_adapter_matches_direct_chain(harness, inputs, tmp_path, mode):
         if mode != 0:
             ev = np.fromfile(tmp_path / f"evals_{run}.bin", dtype=np.float32).reshape(ref["evals"][run].shape)
             assert np.array_equal(ev, ref["evals"][run])
+        if mode != 0:
+            fft = np.fromfile(tmp_path / f"fft_{run}.bin", dtype=np.float32).reshape(ref["fft"][run].shape)
+            assert np.array_equal(fft, ref["fft"][run]), f"spectra of run {run}"
         if mode == 2:
             cnt = np.fromfile(tmp_path / f"counts_{run}.bin", dtype=np.int32).reshape(C, 2)
             assert np.array_equal(cnt, ref["counts"][run])
@@ -128,6 +140,26 @@ def test_adapter_matches_direct_chain(harness, inputs, tmp_path, mode):
     assert proto["vis_missing"] == [1] and proto["vis_total"] == [2 * C * P * F]
     assert proto["vis_start"] == [1000] and proto["vis_end"] == [2999]
     assert proto["status"] == [0]
+    # spectra tails land once per run, in each reference pipeline's order
+    assert proto["fft_done"] == [0 if mode == 0 else 2]
+    run_order = {0: ["beam"], 1: ["beam", "eig", "fft"], 2: ["beam", "fft", "eig"]}[mode]
+    assert proto["order"] == run_order * 2
+
+
+def test_adapter_spectra_match_oracle(harness, inputs, tmp_path):
+    """The landed spectra of both tails against the oracle's transforms of
+    the landed fp16 beams."""
+    for mode in (1, 2):
+        _run(harness, mode, inputs, tmp_path)
+        slots = 2 if mode == 2 else 1
+        for run in range(2):
+            beams = np.fromfile(tmp_path / f"beams_{run}.bin", dtype=np.float16).reshape(
+                C, 2, slots * B, P * TP, 2)
+            bc = orc.beams_from_half(beams)
+            ref = orc.beam_spectra(bc, FFT_DOWNSAMPLE) if mode == 1 else orc.packet_spectra(bc, TP, FFT_TRIM)
+            got = np.fromfile(tmp_path / f"fft_{run}.bin", dtype=np.float32).reshape(ref.shape)
+            m = np.abs(ref).mean(axis=-1, keepdims=True)
+            assert np.all(np.abs(got - ref) <= 2e-5 * m + 1e-6 * np.abs(ref))
 
 
 def test_adapter_visibilities_match_oracle(harness, inputs, tmp_path):
