@@ -49,6 +49,7 @@ void free_plan(sf_plan *p) {
   cudaFree(p->d_weights);
   cudaFree(p->d_weff);
   cudaFree(p->d_spec_tw);
+  cudaFree(p->d_packet_dft);
   cudaFree(p->d_fixed_counts);
   cudaFree(p->d_vis);
   cudaFree(p->d_evals);
@@ -175,6 +176,7 @@ int sf_plan_create(const sf_shape *shape, sf_plan **out_plan) {
   SF_ALLOC(p->d_counts, sizeof(int32_t) * C * 2);
   SF_ALLOC(p->d_status, sizeof(uint32_t));
   if (sf_beam_spectra_supported(p->T)) SF_ALLOC(p->d_spec_tw, sizeof(float2) * p->T);
+  if (p->Tp == 64) SF_ALLOC(p->d_packet_dft, sf_packet_dft_bytes());
 #undef SF_ALLOC
   cudaError_t ez = cudaSuccess;
   ez = ez != cudaSuccess ? ez : cudaMemset(p->d_off_packet, 0, sizeof(int32_t) * p->F);
@@ -183,6 +185,7 @@ int sf_plan_create(const sf_shape *shape, sf_plan **out_plan) {
   ez = ez != cudaSuccess ? ez : cudaMemset(p->d_fixed_counts, 0, sizeof(int32_t) * C);
   ez = ez != cudaSuccess ? ez : cudaMemset(p->d_status, 0, sizeof(uint32_t));
   if (p->d_spec_tw) ez = ez != cudaSuccess ? ez : sf_fill_spectra_twiddles(p->d_spec_tw, p->T);
+  if (p->d_packet_dft) ez = ez != cudaSuccess ? ez : sf_fill_packet_dft(p->d_packet_dft);
   if (ez != cudaSuccess) {
     free_plan(p);
     return cuda_err(ez, "initialise plan memory");

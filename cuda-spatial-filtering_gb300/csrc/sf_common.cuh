@@ -153,6 +153,17 @@ SF_DEVICE void bulk_copy_g2s(void *smem_dst, const void *gmem_src, uint32_t byte
       : "memory");
 }
 
+// Tiled 2-D TMA load of one box at element coordinates (x, y) of the tensor
+// map (a __grid_constant__ kernel parameter), completion on an mbarrier
+// transaction count.  x * element size must be a multiple of 16 bytes.
+SF_DEVICE void tma_load_2d(void *smem_dst, const void *tmap, int x, int y, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(smem_dst)),
+      "l"(tmap), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // 4-byte asynchronous global -> shared copy, and an mbarrier arrival that
 // fires once every cp.async this thread issued before it has landed (the
 // arrival is pre-counted in the barrier's expected count).

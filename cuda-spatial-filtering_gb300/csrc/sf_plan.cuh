@@ -38,6 +38,9 @@ struct sf_plan {
   // W_T^k (k < T) for the whole-integration spectra; NULL when T is not a
   // power of two in [64, 16384].
   float2 *d_spec_tw;
+  // The 64-point DFT operand (fp16 hi + lo, swizzled) of the tensor-core
+  // per-packet spectra; NULL unless Tp == 64.
+  uint8_t *d_packet_dft;
 
   // Scratch for the whole-chain entry points.
   int32_t *d_vis;      // [C][NBL][2][2][2]
@@ -79,6 +82,9 @@ cudaError_t sf_launch_vis_to_float(const sf_plan *p, const int64_t *accum, float
 int sf_beam_spectra_supported(int T);
 int sf_packet_spectra_supported(int Tp);
 cudaError_t sf_fill_spectra_twiddles(float2 *d_tw, int T);
+int sf_packet_spectra_tc_supported(const sf_plan *p);
+size_t sf_packet_dft_bytes();
+cudaError_t sf_fill_packet_dft(uint8_t *d_img);
 cudaError_t sf_launch_beam_spectra(const sf_plan *p, const __half2 *beams, int n_beams_out,
                                    int downsample, float *out, cudaStream_t stream);
 cudaError_t sf_launch_packet_spectra(const sf_plan *p, const __half2 *beams, int n_beams_out,

@@ -29,6 +29,10 @@
 // W_N = exp(-2 pi i / N), in fp32, with twiddles rounded from double precision
 // on the host.
 #include <cmath>
+#include <cstring>
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include "sf_common.cuh"
 #include "sf_plan.cuh"
@@ -102,7 +106,7 @@ constexpr int BS_MAX_LOG2T = 14;
 
 struct BeamSpecArgs {
   const __half2 *beams;  // [S][T]
-  const float2 *tw;      // W_T^k, k < T
+  const float2 *tw;      // per-pass twiddles, see sf_fill_spectra_twiddles
   float *out;            // [S][T / D]
   int S, D;
   Tw64 w;
@@ -117,7 +121,9 @@ SF_DEVICE int bs_swz(int i) { return i ^ ((i >> 4) & 15); }
 // x[j + r T / R] (r < R), multiplies by W_{NS R}^{r (j mod NS)}, transforms over
 // r and writes x[(j / NS) NS R + j mod NS + r NS].  In place: every value is in
 // registers before the barrier, and written after it.  The first pass reads
-// the fp16 series from global memory instead.
+// the fp16 series from global memory instead.  The pass's twiddles sit at
+// tw[NS - 1 + (r - 1) NS + j mod NS], so the lanes of a warp read consecutive
+// entries.
 template <int T, int R, int NS>
 SF_DEVICE void stockham_pass(float2 *x, const __half2 *src, const float2 *tw, const Tw64 &w) {
   constexpr int LOG2R = ilog2c(R);
@@ -141,7 +147,7 @@ SF_DEVICE void stockham_pass(float2 *x, const __half2 *src, const float2 *tw, co
       const int jm = j & (NS - 1);
       if (NS > 1) {
 #pragma unroll
-        for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], __ldg(tw + r * jm * (T / (NS * R))));
+        for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], __ldg(tw + (NS - 1) + (r - 1) * NS + jm));
       }
       dft_reg<LOG2R>(v[b], w);
       const int base = (j - jm) * R + jm;
@@ -305,9 +311,253 @@ __global__ void __launch_bounds__(PK_WARPS * 32, 1) sf_packet_spectra_kernel(con
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Per-packet spectra on the tensor cores (Tp = 64, P a multiple of 32)
+// ---------------------------------------------------------------------------
+// The 64-point DFT of every packet is one GEMM row: with the packet's 64
+// complex fp16 samples as a K = 128 row (re, im interleaved, exactly the
+// beams' memory layout) and the DFT as a 128 x 128 real matrix
+//   B[2t][2f] = cos, B[2t+1][2f] = sin, B[2t][2f+1] = -sin, B[2t+1][2f+1] = cos
+// (angle 2 pi f t / 64), D = A B holds Re X[f], Im X[f] at columns 2f, 2f+1.
+// A tile is 128 packets (rows), loaded by TMA straight from the beams with the
+// 128-byte swizzle (two 16 KB boxes, K halves); B is split into fp16 hi + lo
+// parts (B = hi + lo to ~2^-22) and both are accumulated, so the result equals
+// the fp32 DFT of the fp16 beams to fp32 accumulation error.
+//
+// Warp roles: warps 0-7 epilogue (TMEM lane quarter warp % 4, frequency half
+// warp / 4), warp 8 TMA producer, warp 9 MMA issuer and TMEM owner.  Each
+// persistent CTA owns a contiguous range of series, so every 32-row group of a
+// tile belongs to one series (P % 32 == 0).  The epilogue forms |X| per row,
+// sums each group's 32 rows in shared memory in row order, and warps 0 and 4
+// add the group sums in group order into a running per-series sum in registers:
+// the summation order is fixed, the output deterministic.
+constexpr int TC_EPI_WARPS = 8;
+constexpr int TC_WARP_TMA = 8;
+constexpr int TC_WARP_MMA = 9;
+constexpr int TC_THREADS = 320;
+constexpr int TC_STAGES = 3;
+constexpr uint32_t TC_ATOM = 128 * 128;          // one K half of a tile: 128 rows x 128 B
+constexpr uint32_t TC_TILE_BYTES = 2 * TC_ATOM;   // 128 packets x 256 B
+constexpr uint32_t TC_B_BYTES = 2 * TC_TILE_BYTES;  // hi and lo DFT matrices
+constexpr int TC_RED_STRIDE = 33;
+constexpr uint32_t TC_SUSPEND_NS = 20000;
+
+struct TcHeader {
+  uint64_t a_full[TC_STAGES];
+  uint64_t a_empty[TC_STAGES];
+  uint64_t acc_full[2];
+  uint64_t acc_empty[2];
+  uint64_t b_full;
+  uint64_t mma_done;
+  uint32_t tmem_base;
+  int abort;
+};
+
+struct TcSpecArgs {
+  const uint8_t *dft;  // the B image (hi, lo), TC_B_BYTES, already swizzled
+  float *out;          // [S][64 - 2 trim]
+  uint32_t *status;
+  int S, P, trim;
+};
+
+SF_DEVICE float sqrt_approx(float x) {
+  float y;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    sf_packet_spectra_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcSpecArgs a) {
+  extern __shared__ uint8_t smem_raw[];
+  // 1024-byte alignment for the swizzled operand atoms
+  uint8_t *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+  uint8_t *b_img = smem;                                     // TC_B_BYTES
+  uint8_t *a_stage = b_img + TC_B_BYTES;                     // TC_STAGES x TC_TILE_BYTES
+  float *red = reinterpret_cast<float *>(a_stage + TC_STAGES * TC_TILE_BYTES);  // [8][32][33]
+  float *slot = red + TC_EPI_WARPS * 32 * TC_RED_STRIDE;     // [2][8][32]
+  TcHeader &h = *reinterpret_cast<TcHeader *>(slot + 2 * TC_EPI_WARPS * 32);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // this CTA's series [s0, s1) and its 32-row groups
+  const int s0 = (int)((long long)blockIdx.x * a.S / gridDim.x);
+  const int s1 = (int)((long long)(blockIdx.x + 1) * a.S / gridDim.x);
+  const int n_groups = (s1 - s0) * (a.P / 32);
+  const int n_tiles = (n_groups + 3) / 4;
+  const int row0 = s0 * a.P;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < TC_STAGES; ++i) {
+      mbar_init(&h.a_full[i], 1);
+      mbar_init(&h.a_empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&h.acc_full[i], 1);
+      mbar_init(&h.acc_empty[i], TC_EPI_WARPS);
+    }
+    mbar_init(&h.b_full, 1);
+    mbar_init(&h.mma_done, 1);
+    h.abort = 0;
+    fence_mbarrier_init();
+  }
+  if (warp == TC_WARP_MMA) {
+    tmem_alloc(&h.tmem_base, 256);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  volatile int *abort_flag = &h.abort;
+
+  if (warp == TC_WARP_TMA) {
+    // ---------------- producer ----------------
+    if (lane == 0) {
+      mbar_arrive_expect_tx(&h.b_full, TC_B_BYTES);
+      for (int q = 0; q < 4; ++q)
+        bulk_copy_g2s(b_img + q * (TC_B_BYTES / 4), a.dft + q * (TC_B_BYTES / 4), TC_B_BYTES / 4, &h.b_full);
+      int i = 0;
+      bool stop = false;
+      for (; i < n_tiles; ++i) {
+        const int st = i % TC_STAGES, it = i / TC_STAGES;
+        if (!mbar_wait(&h.a_empty[st], (it & 1) ^ 1, abort_flag, TC_SUSPEND_NS)) {
+          stop = true;
+          break;
+        }
+        uint8_t *dst = a_stage + st * TC_TILE_BYTES;
+        mbar_arrive_expect_tx(&h.a_full[st], TC_TILE_BYTES);
+        tma_load_2d(dst, &tmap, 0, row0 + 128 * i, &h.a_full[st]);
+        tma_load_2d(dst + TC_ATOM, &tmap, 64, row0 + 128 * i, &h.a_full[st]);
+      }
+      // every issued copy lands before shared memory is released
+      mbar_wait_drain(&h.b_full, 0);
+      for (int j = i > TC_STAGES ? i - TC_STAGES : 0; j < i; ++j)
+        mbar_wait_drain(&h.a_full[j % TC_STAGES], (j / TC_STAGES) & 1);
+      if (stop) atomicOr(a.status, SF_DEVERR_TIMEOUT_TMA);
+    }
+  } else if (warp == TC_WARP_MMA) {
+    // ---------------- UMMA issuer ----------------
+    if (lane == 0) {
+      const uint32_t idesc = umma_idesc_f16_f32(128, 128);
+      const uint64_t d_a0 = umma_desc_sw128(smem_u32(a_stage));
+      const uint64_t d_b0 = umma_desc_sw128(smem_u32(b_img));
+      bool failed = !mbar_wait(&h.b_full, 0, abort_flag, TC_SUSPEND_NS);
+      tc_fence_after();
+      for (int i = 0; i < n_tiles; ++i) {
+        const int st = i % TC_STAGES, it = i / TC_STAGES, buf = i & 1;
+        bool ok = mbar_wait(&h.a_full[st], it & 1, abort_flag, TC_SUSPEND_NS);
+        ok = mbar_wait(&h.acc_empty[buf], ((i >> 1) & 1) ^ 1, abort_flag, TC_SUSPEND_NS) && ok;
+        tc_fence_after();
+        failed |= !ok;
+        const uint32_t go = (ok && !failed) ? 1u : 0u;
+        const uint32_t d = h.tmem_base + buf * 128;
+        const uint64_t da = d_a0 + ((st * TC_TILE_BYTES) >> 4);
+#pragma unroll
+        for (int ks = 0; ks < 8; ++ks) {
+          const uint32_t kof = ((ks >> 2) * TC_ATOM + (ks & 3) * 32) >> 4;
+          umma_f16_if(d, da + kof, d_b0 + kof, idesc, ks > 0 ? 1u : 0u, go);
+          umma_f16_if(d, da + kof, d_b0 + ((TC_TILE_BYTES >> 4) + kof), idesc, 1u, go);
+        }
+        umma_commit(&h.a_empty[st]);
+        umma_commit(&h.acc_full[buf]);
+      }
+      umma_commit(&h.mma_done);
+      mbar_wait_drain(&h.mma_done, 0);
+      if (failed) atomicOr(a.status, SF_DEVERR_TIMEOUT_MMA);
+    }
+  } else {
+    // ---------------- epilogue ----------------
+    const int q = warp & 3, half = warp >> 2;
+    const uint32_t tmem = h.tmem_base + (static_cast<uint32_t>(q * 32) << 16) + half * 64;
+    float *my_red = red + warp * 32 * TC_RED_STRIDE;
+    const int W = 64 - 2 * a.trim;
+    const int hi0 = 32 + a.trim, lo_end = 32 - a.trim;
+    const int f = half * 32 + lane;  // frequency this lane reduces and writes
+    const int g_out = f >= hi0 ? f - hi0 : (f < lo_end ? f + lo_end : -1);
+    const int groups_per_series = a.P / 32;
+    float cur = 0.f;  // running sum of the current series (warps 0 and 4)
+    bool failed = false;
+    for (int i = 0; i < n_tiles; ++i) {
+      const int buf = i & 1;
+      const bool ok = mbar_wait(&h.acc_full[buf], (i >> 1) & 1, abort_flag, TC_SUSPEND_NS);
+      tc_fence_after();
+      failed |= !ok;
+      float mag[32];
+      if (ok) {
+        uint32_t v[4][16];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) tmem_ld16(tmem + buf * 128 + 16 * j, v[j]);
+        tmem_wait_ld();
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+          const float re = __uint_as_float(v[k >> 3][(2 * k) & 15]);
+          const float im = __uint_as_float(v[k >> 3][(2 * k + 1) & 15]);
+          mag[k] = sqrt_approx(re * re + im * im);
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&h.acc_empty[buf]);
+      // this warp's 32 rows: one group of one series
+      const int gi = 4 * i + q;
+      float *my_slot = slot + (buf * TC_EPI_WARPS + warp) * 32;
+      if (ok && gi < n_groups) {
+#pragma unroll
+        for (int k = 0; k < 32; ++k) my_red[lane * TC_RED_STRIDE + k] = mag[k];
+        __syncwarp();
+        float sum = 0.f;
+#pragma unroll 8
+        for (int r = 0; r < 32; ++r) sum += my_red[r * TC_RED_STRIDE + lane];
+        my_slot[lane] = sum;
+        __syncwarp();
+      }
+      named_bar_sync(1, TC_EPI_WARPS * 32);
+      if (q == 0) {
+        // warps 0 and 4: add the tile's four group sums in order
+        for (int qq = 0; qq < 4; ++qq) {
+          const int gq = 4 * i + qq;
+          if (!ok || gq >= n_groups) break;
+          cur += slot[(buf * TC_EPI_WARPS + 4 * half + qq) * 32 + lane];
+          if ((gq + 1) % groups_per_series == 0) {
+            const int s = s0 + gq / groups_per_series;
+            if (g_out >= 0) a.out[(size_t)s * W + g_out] = cur;
+            cur = 0.f;
+          }
+        }
+      }
+    }
+    if (failed && lane == 0) atomicOr(a.status, SF_DEVERR_TIMEOUT_EPILOGUE);
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == TC_WARP_MMA) {
+    tc_fence_after();
+    tmem_dealloc(h.tmem_base, 256);
+  }
+}
+
+size_t tc_smem_bytes() {
+  return 1024 + TC_B_BYTES + TC_STAGES * TC_TILE_BYTES + sizeof(float) * TC_EPI_WARPS * 32 * TC_RED_STRIDE +
+         sizeof(float) * 2 * TC_EPI_WARPS * 32 + sizeof(TcHeader);
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
 constexpr int MAX_DEVICES = 64;
 bool g_bs_attr[MAX_DEVICES][BS_MAX_LOG2T + 1];
 bool g_pk_attr[MAX_DEVICES][7];
+bool g_tc_attr[MAX_DEVICES];
 
 template <typename K>
 cudaError_t ensure_smem(K kernel, bool &done, size_t smem) {
@@ -352,13 +602,23 @@ int sf_packet_spectra_supported(int Tp) {
   return l >= 4 && l <= 6;
 }
 
+// Twiddles of every Stockham pass of a T-point transform (radix 16 while at
+// least 16 remain, then the remainder): the pass combining sub-transforms of
+// length NS uses W_{NS R}^{r jm} (1 <= r < R, jm < NS) at NS - 1 + (r - 1) NS + jm.
+// The pass blocks telescope: sum (R - 1) NS = T - 1 entries in all.
 cudaError_t sf_fill_spectra_twiddles(float2 *d_tw, int T) {
-  float2 *h = static_cast<float2 *>(malloc(sizeof(float2) * T));
+  float2 *h = static_cast<float2 *>(calloc(T, sizeof(float2)));
   if (!h) return cudaErrorMemoryAllocation;
   const double pi = 3.14159265358979323846;
-  for (int k = 0; k < T; ++k)
-    h[k] = make_float2(static_cast<float>(std::cos(2.0 * pi * k / T)),
-                       static_cast<float>(-std::sin(2.0 * pi * k / T)));
+  for (int ns = 1; ns < T;) {
+    const int r_max = T / ns >= 16 ? 16 : T / ns;
+    for (int r = 1; r < r_max; ++r)
+      for (int jm = 0; jm < ns; ++jm) {
+        const double a = 2.0 * pi * (double)r * jm / ((double)ns * r_max);
+        h[ns - 1 + (r - 1) * ns + jm] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(-std::sin(a)));
+      }
+    ns *= r_max;
+  }
   cudaError_t e = cudaMemcpy(d_tw, h, sizeof(float2) * T, cudaMemcpyHostToDevice);
   free(h);
   return e;
@@ -388,8 +648,65 @@ cudaError_t sf_launch_beam_spectra(const sf_plan *p, const __half2 *beams, int n
   }
 }
 
+int sf_packet_spectra_tc_supported(const sf_plan *p) { return p->Tp == 64 && p->P % 32 == 0; }
+
+// The DFT operand image for the tensor-core path: [hi, lo][K half][128 rows n]
+// [128 B], each row's 16-byte chunks stored at chunk ^ (n % 8) (the 128-byte
+// swizzle), values B[k][n] of the real 128 x 128 form of the 64-point DFT.
+cudaError_t sf_fill_packet_dft(uint8_t *d_img) {
+  uint8_t *h = static_cast<uint8_t *>(calloc(TC_B_BYTES, 1));
+  if (!h) return cudaErrorMemoryAllocation;
+  const double pi = 3.14159265358979323846;
+  for (int n = 0; n < 128; ++n)
+    for (int k = 0; k < 128; ++k) {
+      const int f = n >> 1, c = n & 1, t = k >> 1, d = k & 1;
+      const double ang = 2.0 * pi * (double)((f * t) % 64) / 64.0;
+      const double co = std::cos(ang), si = std::sin(ang);
+      const double v = c == 0 ? (d == 0 ? co : si) : (d == 0 ? -si : co);
+      const __half hi = __double2half(v);
+      const __half lo = __double2half(v - (double)__half2float(hi));
+      const int atom = k >> 6, kk = k & 63;
+      const size_t off = (size_t)atom * TC_ATOM + n * 128 + ((((kk >> 3) ^ (n & 7))) << 4) + (kk & 7) * 2;
+      memcpy(h + off, &hi, 2);
+      memcpy(h + TC_TILE_BYTES + off, &lo, 2);
+    }
+  cudaError_t e = cudaMemcpy(d_img, h, TC_B_BYTES, cudaMemcpyHostToDevice);
+  free(h);
+  return e;
+}
+
+size_t sf_packet_dft_bytes() { return TC_B_BYTES; }
+
 cudaError_t sf_launch_packet_spectra(const sf_plan *p, const __half2 *beams, int n_beams_out,
                                      int trim, float *out, cudaStream_t stream) {
+  if (sf_packet_spectra_tc_supported(p) && p->d_packet_dft) {
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode) return cudaErrorNotSupported;
+    const int S = p->C * 2 * n_beams_out;
+    CUtensorMap tmap;
+    const cuuint64_t dims[2] = {128, (cuuint64_t)S * p->P};
+    const cuuint64_t strides[1] = {256};
+    const cuuint32_t box[2] = {64, 128};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<__half2 *>(beams), dims, strides,
+                        box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+    TcSpecArgs a;
+    a.dft = p->d_packet_dft;
+    a.out = out;
+    a.status = p->d_status;
+    a.S = S;
+    a.P = p->P;
+    a.trim = trim;
+    if (p->device < 0 || p->device >= MAX_DEVICES) return cudaErrorInvalidDevice;
+    const size_t smem = tc_smem_bytes();
+    cudaError_t e = ensure_smem(sf_packet_spectra_tc_kernel, g_tc_attr[p->device], smem);
+    if (e != cudaSuccess) return e;
+    const int grid = S < p->num_sms ? S : p->num_sms;
+    sf_packet_spectra_tc_kernel<<<grid, TC_THREADS, smem, stream>>>(tmap, a);
+    return cudaGetLastError();
+  }
   PacketSpecArgs a;
   a.beams = reinterpret_cast<const uint4 *>(beams);
   a.out = out;

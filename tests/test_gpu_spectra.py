@@ -80,12 +80,14 @@ def test_beam_spectra_nan_series_gives_zero_and_leaves_others():
     _row_close(got[mask], ref[mask], 2e-5, 1e-6)
 
 
-@pytest.mark.parametrize("Tp,P,trim", [
-    (64, 64, 5), (64, 1, 5), (64, 33, 0), (64, 100, 31), (32, 5, 5), (32, 64, 0), (16, 7, 2), (16, 65, 7),
+# Tp = 64 with P % 32 == 0 takes the tensor-core path, the rest the SIMT path
+@pytest.mark.parametrize("Tp,P,trim,C,nb", [
+    (64, 64, 5, 3, 4), (64, 32, 5, 3, 4), (64, 96, 0, 3, 4), (64, 128, 31, 2, 3), (64, 64, 5, 40, 8),
+    (64, 1, 5, 3, 4), (64, 33, 0, 3, 4), (64, 100, 31, 3, 4), (32, 5, 5, 3, 4), (32, 64, 0, 3, 4),
+    (16, 7, 2, 3, 4), (16, 65, 7, 3, 4),
 ])
-def test_packet_spectra_matches_oracle(Tp, P, trim):
-    rng = np.random.default_rng(Tp * 1000 + P)
-    C, nb = 3, 4
+def test_packet_spectra_matches_oracle(Tp, P, trim, C, nb):
+    rng = np.random.default_rng(Tp * 1000 + P + C)
     plan = sfgb.Plan(C, 1, Tp, 4, 4, P, 2)
     beams = _random_beams(rng, C, nb, Tp * P)
     out = torch.full(plan.packet_spectra_shape(nb, trim), -1.0, dtype=torch.float32, device="cuda")
