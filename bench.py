@@ -348,13 +348,22 @@ def _stage_breakdown(plan, d_s, d_sc, vis, ev, cnt, beams, stream, reps, only=No
         for i in range(2):
             fn(i)
         stream.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for i in range(reps):
-            fn(i)
-        e1.record(stream)
+        # the launches replay from a CUDA graph, so short kernels are timed
+        # back to back rather than at the pace of the host's calls
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            for i in range(reps):
+                fn(i)
+        with torch.cuda.stream(stream):  # replay() launches on the current stream
+            g.replay()
+            stream.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.replay()
+            e1.record(stream)
         e1.synchronize()
         out[name] = {"ms": e0.elapsed_time(e1) / reps}
+        del g
     return out
 
 

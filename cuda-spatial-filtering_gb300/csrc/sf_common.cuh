@@ -164,6 +164,14 @@ SF_DEVICE void tma_load_2d(void *smem_dst, const void *tmap, int x, int y, uint6
       : "memory");
 }
 
+SF_DEVICE void tma_load_3d(void *smem_dst, const void *tmap, int x, int y, int z, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+          smem_u32(smem_dst)),
+      "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // 4-byte asynchronous global -> shared copy, and an mbarrier arrival that
 // fires once every cp.async this thread issued before it has landed (the
 // arrival is pre-counted in the barrier's expected count).

@@ -325,29 +325,35 @@ __global__ void __launch_bounds__(PK_WARPS * 32, 1) sf_packet_spectra_kernel(con
 // parts (B = hi + lo to ~2^-22) and both are accumulated, so the result equals
 // the fp32 DFT of the fp16 beams to fp32 accumulation error.
 //
-// Warp roles: warps 0-7 epilogue (TMEM lane quarter warp % 4, frequency half
-// warp / 4), warp 8 TMA producer, warp 9 MMA issuer and TMEM owner.  Each
-// persistent CTA owns a contiguous range of series, so every 32-row group of a
-// tile belongs to one series (P % 32 == 0).  The epilogue forms |X| per row,
-// sums each group's 32 rows in shared memory in row order, and warps 0 and 4
-// add the group sums in group order into a running per-series sum in registers:
-// the summation order is fixed, the output deterministic.
+// A tile holds 32 consecutive packets of 4 series (series-major: TMEM lane
+// 32 q + r is packet r of series q), loaded by one 3-D TMA box per K half.
+// Warp roles: warps 0-7 epilogue (TMEM lane quarter q = warp % 4, frequency
+// half warp / 4), warp 8 TMA producer, warp 9 MMA issuer and TMEM owner.  Each
+// persistent CTA owns a contiguous range of series and walks it 4 series at a
+// time, P / 32 tiles per quad, so epilogue warp q only ever sees series q of
+// the quad: each thread adds its row's |X| into registers tile after tile
+// (packets r, 32 + r, ... of the series), and at the series' last tile the
+// warp sums its 32 rows per frequency in shared memory in row order.  The
+// summation order is fixed, the output deterministic, and no epilogue warp
+// waits for another.
 constexpr int TC_EPI_WARPS = 8;
 constexpr int TC_WARP_TMA = 8;
 constexpr int TC_WARP_MMA = 9;
 constexpr int TC_THREADS = 320;
-constexpr int TC_STAGES = 3;
+constexpr int TC_STAGES = 4;
 constexpr uint32_t TC_ATOM = 128 * 128;          // one K half of a tile: 128 rows x 128 B
 constexpr uint32_t TC_TILE_BYTES = 2 * TC_ATOM;   // 128 packets x 256 B
 constexpr uint32_t TC_B_BYTES = 2 * TC_TILE_BYTES;  // hi and lo DFT matrices
 constexpr int TC_RED_STRIDE = 33;
 constexpr uint32_t TC_SUSPEND_NS = 20000;
 
+constexpr int TC_ACC = 4;  // tensor-memory accumulators (128 columns each): the epilogue may lag 3 tiles
+
 struct TcHeader {
   uint64_t a_full[TC_STAGES];
   uint64_t a_empty[TC_STAGES];
-  uint64_t acc_full[2];
-  uint64_t acc_empty[2];
+  uint64_t acc_full[TC_ACC];
+  uint64_t acc_empty[TC_ACC];
   uint64_t b_full;
   uint64_t mma_done;
   uint32_t tmem_base;
@@ -375,23 +381,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   uint8_t *b_img = smem;                                     // TC_B_BYTES
   uint8_t *a_stage = b_img + TC_B_BYTES;                     // TC_STAGES x TC_TILE_BYTES
   float *red = reinterpret_cast<float *>(a_stage + TC_STAGES * TC_TILE_BYTES);  // [8][32][33]
-  float *slot = red + TC_EPI_WARPS * 32 * TC_RED_STRIDE;     // [2][8][32]
-  TcHeader &h = *reinterpret_cast<TcHeader *>(slot + 2 * TC_EPI_WARPS * 32);
+  TcHeader &h = *reinterpret_cast<TcHeader *>(red + TC_EPI_WARPS * 32 * TC_RED_STRIDE);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // this CTA's series [s0, s1) and its 32-row groups
+  // this CTA's series [s0, s1), walked 4 at a time, P / 32 tiles per quad
   const int s0 = (int)((long long)blockIdx.x * a.S / gridDim.x);
   const int s1 = (int)((long long)(blockIdx.x + 1) * a.S / gridDim.x);
-  const int n_groups = (s1 - s0) * (a.P / 32);
-  const int n_tiles = (n_groups + 3) / 4;
-  const int row0 = s0 * a.P;
+  const int tiles_per_quad = a.P / 32;
+  const int n_tiles = ((s1 - s0 + 3) / 4) * tiles_per_quad;
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < TC_STAGES; ++i) {
       mbar_init(&h.a_full[i], 1);
       mbar_init(&h.a_empty[i], 1);
     }
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < TC_ACC; ++i) {
       mbar_init(&h.acc_full[i], 1);
       mbar_init(&h.acc_empty[i], TC_EPI_WARPS);
     }
@@ -401,7 +405,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     fence_mbarrier_init();
   }
   if (warp == TC_WARP_MMA) {
-    tmem_alloc(&h.tmem_base, 256);
+    tmem_alloc(&h.tmem_base, 128 * TC_ACC);
     tmem_relinquish();
   }
   tc_fence_before();
@@ -423,10 +427,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           stop = true;
           break;
         }
+        const int quad = i / tiles_per_quad, t = i - quad * tiles_per_quad;
         uint8_t *dst = a_stage + st * TC_TILE_BYTES;
         mbar_arrive_expect_tx(&h.a_full[st], TC_TILE_BYTES);
-        tma_load_2d(dst, &tmap, 0, row0 + 128 * i, &h.a_full[st]);
-        tma_load_2d(dst + TC_ATOM, &tmap, 64, row0 + 128 * i, &h.a_full[st]);
+        tma_load_3d(dst, &tmap, 0, 32 * t, s0 + 4 * quad, &h.a_full[st]);
+        tma_load_3d(dst + TC_ATOM, &tmap, 64, 32 * t, s0 + 4 * quad, &h.a_full[st]);
       }
       // every issued copy lands before shared memory is released
       mbar_wait_drain(&h.b_full, 0);
@@ -440,12 +445,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const uint32_t idesc = umma_idesc_f16_f32(128, 128);
       const uint64_t d_a0 = umma_desc_sw128(smem_u32(a_stage));
       const uint64_t d_b0 = umma_desc_sw128(smem_u32(b_img));
-      bool failed = !mbar_wait(&h.b_full, 0, abort_flag, TC_SUSPEND_NS);
+      bool failed = !mbar_wait(&h.b_full, 0, abort_flag);
       tc_fence_after();
       for (int i = 0; i < n_tiles; ++i) {
-        const int st = i % TC_STAGES, it = i / TC_STAGES, buf = i & 1;
-        bool ok = mbar_wait(&h.a_full[st], it & 1, abort_flag, TC_SUSPEND_NS);
-        ok = mbar_wait(&h.acc_empty[buf], ((i >> 1) & 1) ^ 1, abort_flag, TC_SUSPEND_NS) && ok;
+        const int st = i % TC_STAGES, it = i / TC_STAGES, buf = i % TC_ACC;
+        bool ok = mbar_wait(&h.a_full[st], it & 1, abort_flag);
+        ok = mbar_wait(&h.acc_empty[buf], ((i / TC_ACC) & 1) ^ 1, abort_flag) && ok;
         tc_fence_after();
         failed |= !ok;
         const uint32_t go = (ok && !failed) ? 1u : 0u;
@@ -473,56 +478,49 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int hi0 = 32 + a.trim, lo_end = 32 - a.trim;
     const int f = half * 32 + lane;  // frequency this lane reduces and writes
     const int g_out = f >= hi0 ? f - hi0 : (f < lo_end ? f + lo_end : -1);
-    const int groups_per_series = a.P / 32;
-    float cur = 0.f;  // running sum of the current series (warps 0 and 4)
+    float acc[32];  // this row's |X| summed over the series' tiles
+#pragma unroll
+    for (int k = 0; k < 32; ++k) acc[k] = 0.f;
     bool failed = false;
     for (int i = 0; i < n_tiles; ++i) {
-      const int buf = i & 1;
-      const bool ok = mbar_wait(&h.acc_full[buf], (i >> 1) & 1, abort_flag, TC_SUSPEND_NS);
+      const int buf = i % TC_ACC;
+      const int quad = i / tiles_per_quad, t = i - quad * tiles_per_quad;
+      const int s = s0 + 4 * quad + q;
+      const bool ok = mbar_wait(&h.acc_full[buf], (i / TC_ACC) & 1, abort_flag);
       tc_fence_after();
       failed |= !ok;
-      float mag[32];
+      uint32_t v[4][16];  // Re, Im of this row's 32 frequencies
       if (ok) {
-        uint32_t v[4][16];
 #pragma unroll
         for (int j = 0; j < 4; ++j) tmem_ld16(tmem + buf * 128 + 16 * j, v[j]);
         tmem_wait_ld();
+      }
+      // the tile is in registers: hand the accumulator back before the math
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&h.acc_empty[buf]);
+      if (ok) {
 #pragma unroll
         for (int k = 0; k < 32; ++k) {
           const float re = __uint_as_float(v[k >> 3][(2 * k) & 15]);
           const float im = __uint_as_float(v[k >> 3][(2 * k + 1) & 15]);
-          mag[k] = sqrt_approx(re * re + im * im);
+          acc[k] += sqrt_approx(re * re + im * im);
         }
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&h.acc_empty[buf]);
-      // this warp's 32 rows: one group of one series
-      const int gi = 4 * i + q;
-      float *my_slot = slot + (buf * TC_EPI_WARPS + warp) * 32;
-      if (ok && gi < n_groups) {
+      if (t == tiles_per_quad - 1) {
+        // series done: sum the 32 rows (packets r, 32 + r, ...) per frequency in row order
+        if (ok && s < s1) {
 #pragma unroll
-        for (int k = 0; k < 32; ++k) my_red[lane * TC_RED_STRIDE + k] = mag[k];
-        __syncwarp();
-        float sum = 0.f;
-#pragma unroll 8
-        for (int r = 0; r < 32; ++r) sum += my_red[r * TC_RED_STRIDE + lane];
-        my_slot[lane] = sum;
-        __syncwarp();
-      }
-      named_bar_sync(1, TC_EPI_WARPS * 32);
-      if (q == 0) {
-        // warps 0 and 4: add the tile's four group sums in order
-        for (int qq = 0; qq < 4; ++qq) {
-          const int gq = 4 * i + qq;
-          if (!ok || gq >= n_groups) break;
-          cur += slot[(buf * TC_EPI_WARPS + 4 * half + qq) * 32 + lane];
-          if ((gq + 1) % groups_per_series == 0) {
-            const int s = s0 + gq / groups_per_series;
-            if (g_out >= 0) a.out[(size_t)s * W + g_out] = cur;
-            cur = 0.f;
-          }
+          for (int k = 0; k < 32; ++k) my_red[lane * TC_RED_STRIDE + k] = acc[k];
+          __syncwarp();
+          float part[4] = {0.f, 0.f, 0.f, 0.f};  // rows r = 4 m + j into part[j]
+#pragma unroll
+          for (int r = 0; r < 32; ++r) part[r & 3] += my_red[r * TC_RED_STRIDE + lane];
+          __syncwarp();
+          if (g_out >= 0) a.out[(size_t)s * W + g_out] = (part[0] + part[1]) + (part[2] + part[3]);
         }
+#pragma unroll
+        for (int k = 0; k < 32; ++k) acc[k] = 0.f;
       }
     }
     if (failed && lane == 0) atomicOr(a.status, SF_DEVERR_TIMEOUT_EPILOGUE);
@@ -532,13 +530,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   __syncthreads();
   if (warp == TC_WARP_MMA) {
     tc_fence_after();
-    tmem_dealloc(h.tmem_base, 256);
+    tmem_dealloc(h.tmem_base, 128 * TC_ACC);
   }
 }
 
 size_t tc_smem_bytes() {
   return 1024 + TC_B_BYTES + TC_STAGES * TC_TILE_BYTES + sizeof(float) * TC_EPI_WARPS * 32 * TC_RED_STRIDE +
-         sizeof(float) * 2 * TC_EPI_WARPS * 32 + sizeof(TcHeader);
+         sizeof(TcHeader);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
@@ -684,11 +682,12 @@ cudaError_t sf_launch_packet_spectra(const sf_plan *p, const __half2 *beams, int
     if (!encode) return cudaErrorNotSupported;
     const int S = p->C * 2 * n_beams_out;
     CUtensorMap tmap;
-    const cuuint64_t dims[2] = {128, (cuuint64_t)S * p->P};
-    const cuuint64_t strides[1] = {256};
-    const cuuint32_t box[2] = {64, 128};
-    const cuuint32_t estr[2] = {1, 1};
-    CUresult r = encode(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<__half2 *>(beams), dims, strides,
+    // [series][packet][128 fp16]; a box is 4 series x 32 packets x one K half
+    const cuuint64_t dims[3] = {128, (cuuint64_t)p->P, (cuuint64_t)S};
+    const cuuint64_t strides[2] = {256, (cuuint64_t)p->P * 256};
+    const cuuint32_t box[3] = {64, 32, 4};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = encode(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<__half2 *>(beams), dims, strides,
                         box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
