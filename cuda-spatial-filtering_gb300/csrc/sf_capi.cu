@@ -50,6 +50,11 @@ void free_plan(sf_plan *p) {
   cudaFree(p->d_weff);
   cudaFree(p->d_spec_tw);
   cudaFree(p->d_packet_dft);
+  cudaFree(p->d_steer);
+  cudaFree(p->d_steer_conn);
+  cudaFree(p->d_steer_cal);
+  free(p->h_steer);
+  free(p->h_steer_conn);
   cudaFree(p->d_fixed_counts);
   cudaFree(p->d_vis);
   cudaFree(p->d_evals);
@@ -150,7 +155,10 @@ int sf_plan_create(const sf_shape *shape, sf_plan **out_plan) {
   p->h_phasors = static_cast<float2 *>(malloc(sizeof(float2) * C * R));
   p->h_factors = static_cast<float2 *>(malloc(sizeof(float2) * C * 2 * R));
   p->h_fixed_counts = static_cast<int32_t *>(calloc(C, sizeof(int32_t)));
-  if (!p->h_delays || !p->h_gains || !p->h_phasors || !p->h_factors || !p->h_fixed_counts) {
+  p->h_steer = static_cast<double *>(calloc(3 * (B + R), sizeof(double)));
+  p->h_steer_conn = static_cast<int32_t *>(calloc(R, sizeof(int32_t)));
+  if (!p->h_delays || !p->h_gains || !p->h_phasors || !p->h_factors || !p->h_fixed_counts || !p->h_steer ||
+      !p->h_steer_conn) {
     free_plan(p);
     return set_err(SF_ERR_INVALID_ARGUMENT, "out of host memory");
   }
@@ -177,6 +185,9 @@ int sf_plan_create(const sf_shape *shape, sf_plan **out_plan) {
   SF_ALLOC(p->d_status, sizeof(uint32_t));
   if (sf_beam_spectra_supported(p->T)) SF_ALLOC(p->d_spec_tw, sizeof(float2) * p->T);
   if (p->Tp == 64) SF_ALLOC(p->d_packet_dft, sf_packet_dft_bytes());
+  SF_ALLOC(p->d_steer, sizeof(double) * 3 * (B + R));
+  SF_ALLOC(p->d_steer_conn, sizeof(int32_t) * R);
+  SF_ALLOC(p->d_steer_cal, sizeof(float2) * C * 2 * R);
 #undef SF_ALLOC
   cudaError_t ez = cudaSuccess;
   ez = ez != cudaSuccess ? ez : cudaMemset(p->d_off_packet, 0, sizeof(int32_t) * p->F);
@@ -314,6 +325,37 @@ int sf_set_weights(sf_plan *plan, const uint16_t *h_weights_f16, void *stream) {
   SF_TRY(cudaMemcpyAsync(plan->d_weights, h_weights_f16, bytes, cudaMemcpyHostToDevice, s),
          "weights upload");
   SF_TRY(cudaStreamSynchronize(s), "weights upload");
+  return SF_OK;
+}
+
+int sf_set_steering_weights(sf_plan *plan, const double *h_dircos, const double *h_enu, const int32_t *h_connected,
+                            double base_freq_hz, double channel_bw_hz, int32_t min_freq_ch, const float *h_cal_gains,
+                            void *stream) {
+  if (int rc = check_plan(plan)) return rc;
+  if (!h_dircos || !h_enu) return set_err(SF_ERR_INVALID_ARGUMENT, "direction cosines / antenna positions are NULL");
+  const int B = plan->B, R = plan->R;
+  for (int i = 0; i < 3 * B; ++i)
+    if (!std::isfinite(h_dircos[i])) return set_err(SF_ERR_INVALID_ARGUMENT, "direction cosine %d is not finite", i);
+  for (int i = 0; i < 3 * R; ++i)
+    if (!std::isfinite(h_enu[i])) return set_err(SF_ERR_INVALID_ARGUMENT, "antenna coordinate %d is not finite", i);
+  if (!std::isfinite(base_freq_hz) || !std::isfinite(channel_bw_hz))
+    return set_err(SF_ERR_INVALID_ARGUMENT, "frequency plan is not finite");
+  // stage in plan-owned host memory: the caller's arrays are free on return
+  memcpy(plan->h_steer, h_dircos, sizeof(double) * 3 * B);
+  memcpy(plan->h_steer + 3 * B, h_enu, sizeof(double) * 3 * R);
+  for (int r = 0; r < R; ++r) plan->h_steer_conn[r] = h_connected ? (h_connected[r] != 0) : 1;
+  cudaStream_t s = as_stream(stream);
+  SF_TRY(cudaMemcpyAsync(plan->d_steer, plan->h_steer, sizeof(double) * 3 * (B + R), cudaMemcpyHostToDevice, s),
+         "steering upload");
+  SF_TRY(cudaMemcpyAsync(plan->d_steer_conn, plan->h_steer_conn, sizeof(int32_t) * R, cudaMemcpyHostToDevice, s),
+         "steering upload");
+  if (h_cal_gains)
+    SF_TRY(cudaMemcpyAsync(plan->d_steer_cal, h_cal_gains, sizeof(float2) * plan->C * 2 * R, cudaMemcpyHostToDevice, s),
+           "calibration upload");
+  SF_TRY(sf_launch_steering(plan, plan->d_steer, plan->d_steer + 3 * B, plan->d_steer_conn,
+                            h_cal_gains ? plan->d_steer_cal : nullptr, base_freq_hz, channel_bw_hz, min_freq_ch, s),
+         "steering launch");
+  SF_TRY(cudaStreamSynchronize(s), "steering synthesis");
   return SF_OK;
 }
 

@@ -42,6 +42,14 @@ struct sf_plan {
   // per-packet spectra; NULL unless Tp == 64.
   uint8_t *d_packet_dft;
 
+  // Steering-synthesis inputs: [B][3] direction cosines then [R][3] antenna
+  // positions (doubles), [R] connected flags, [C][2][R] calibration gains.
+  double *d_steer;
+  int32_t *d_steer_conn;
+  float2 *d_steer_cal;
+  double *h_steer;
+  int32_t *h_steer_conn;
+
   // Scratch for the whole-chain entry points.
   int32_t *d_vis;      // [C][NBL][2][2][2]
   float *d_evals;      // [C][2][2][R]
@@ -77,6 +85,11 @@ cudaError_t sf_launch_vis_accumulate(const sf_plan *p, const int32_t *vis, int64
                                      cudaStream_t stream);
 cudaError_t sf_launch_vis_to_float(const sf_plan *p, const int64_t *accum, float *out,
                                    cudaStream_t stream);
+
+// Steering-weight synthesis (sf_steering.cu).
+cudaError_t sf_launch_steering(const sf_plan *p, const double *d_dircos, const double *d_enu,
+                               const int32_t *d_connected, const float2 *d_cal, double base_hz, double bw_hz,
+                               int min_ch, cudaStream_t stream);
 
 // Beam spectra (sf_spectra.cu).
 int sf_beam_spectra_supported(int T);

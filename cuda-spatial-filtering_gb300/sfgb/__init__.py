@@ -60,6 +60,7 @@ _SIGS = {
     "sf_set_fine_delays": ([_P, _P, ctypes.c_double, ctypes.c_double, _I32, _P], ctypes.c_int),
     "sf_set_weights": ([_P, _P, _P], ctypes.c_int),
     "sf_set_fixed_counts": ([_P, _P, _P], ctypes.c_int),
+    "sf_set_steering_weights": ([_P, _P, _P, _P, ctypes.c_double, ctypes.c_double, _I32, _P, _P], ctypes.c_int),
     "sf_set_stream_permutation": ([_P, _P, _P, _P], ctypes.c_int),
     "sf_correlate": ([_P, _P, _P, _I32, _P, _P], ctypes.c_int),
     "sf_covariance_eig": ([_P, _P, _I32, _I32, ctypes.c_float, _I32, _P, _P, _P, _P, _P], ctypes.c_int),
@@ -203,6 +204,23 @@ class Plan:
             raise ValueError("set_stream_permutation: size must equal 2 x receivers")
         _check(lib().sf_set_stream_permutation(self._h, rp.ctypes.data_as(_P), pp.ctypes.data_as(_P),
                                                _stream(stream)))
+
+    def set_steering_weights(self, dircos, enu, connected=None, base_freq_hz=0.0, channel_bw_hz=0.0,
+                             min_freq_ch=0, calibration_gains=None, stream=None):
+        """Weights synthesised on the device from direction cosines [B][3] and
+        antenna positions [R][3] (ENU metres); connected[r] == 0 marks a null
+        input; calibration_gains complex [C][Pol][R] or None."""
+        dc = np.ascontiguousarray(dircos, dtype=np.float64).reshape(self.B, 3)
+        pos = np.ascontiguousarray(enu, dtype=np.float64).reshape(self.R, 3)
+        conn = None if connected is None else np.ascontiguousarray(connected, dtype=np.int32).reshape(self.R)
+        cal = None
+        if calibration_gains is not None:
+            g = np.asarray(calibration_gains).reshape(self.C, 2, self.R)
+            cal = np.ascontiguousarray(np.stack([g.real, g.imag], axis=-1).astype(np.float32))
+        _check(lib().sf_set_steering_weights(
+            self._h, dc.ctypes.data_as(_P), pos.ctypes.data_as(_P), None if conn is None else conn.ctypes.data_as(_P),
+            float(base_freq_hz), float(channel_bw_hz), int(min_freq_ch),
+            None if cal is None else cal.ctypes.data_as(_P), _stream(stream)))
 
     def set_fixed_counts(self, counts=None, stream=None):
         arr = None if counts is None else np.ascontiguousarray(counts, dtype=np.int32)

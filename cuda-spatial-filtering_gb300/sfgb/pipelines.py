@@ -74,10 +74,59 @@ class SingleHostMemoryOutput:
         return 1
 
 
+class BeamSteering:
+    """BeamSteering mirror (include/spatial/pipeline/common.hpp:187-327): keeps
+    every registered plan's weights pointed at the targets, recomputed on the
+    device (Plan.set_steering_weights) at most once per update interval.
+    Inert without targets.  targets: list of dicts {"mode": "zenith"|"radec",
+    "ra_deg", "dec_deg"}; antenna_positions: {antenna id: (east, north, up)};
+    antenna_mapping: {receiver index: antenna id} (negative = null input);
+    calibration_gains: complex [C][Pol][R] or None."""
+
+    def __init__(self, targets, antenna_positions, antenna_mapping, base_frequency_hz, channel_bandwidth_hz,
+                 min_freq_channel, latitude_deg=0.0, longitude_deg=0.0, height_m=0.0,
+                 update_interval_seconds=180.0, calibration_gains=None, clock=None):
+        import time
+        self.targets = list(targets or [])
+        self.positions = dict(antenna_positions or {})
+        self.mapping = dict(antenna_mapping or {})
+        self.base, self.bw, self.min_ch = float(base_frequency_hz), float(channel_bandwidth_hz), int(min_freq_channel)
+        self.site = (float(latitude_deg), float(longitude_deg), float(height_m))
+        self.interval = float(update_interval_seconds)
+        self.cal = calibration_gains
+        self.clock = clock or time.time
+        self.plans = []
+        self.last_update = None
+
+    def active(self):
+        return bool(self.targets)
+
+    def register_plan(self, plan, stream=None):
+        self.plans.append((plan, stream))
+
+    def refresh(self, unix_seconds):
+        from . import pointing
+        for plan, stream in self.plans:
+            dircos, enu, conn = pointing.steering_geometry(plan.B, plan.R, self.targets, self.positions,
+                                                           self.mapping, unix_seconds, *self.site)
+            plan.set_steering_weights(dircos, enu, conn, self.base, self.bw, self.min_ch, self.cal, stream=stream)
+        self.last_update = unix_seconds
+
+    def maybe_refresh(self):
+        if not self.active() or not self.plans:
+            return False
+        now = self.clock()
+        if self.last_update is not None and now - self.last_update < self.interval:
+            return False
+        self.refresh(now)
+        return True
+
+
 class GPUPipeline:
     def __init__(self):
         self.state_ = None
         self.output_ = None
+        self.steering_ = None
 
     def set_state(self, state):
         self.state_ = state
@@ -100,6 +149,10 @@ class GPUPipeline:
             raise RuntimeError("set_stream_permutation: size must equal NR_FPGA_SOURCES * "
                                "NR_RECEIVERS_PER_PACKET * NR_POLARIZATIONS")
         self.plan.set_stream_permutation(recv_perm, pol_perm)
+
+    def set_beam_steering(self, steering):
+        self.steering_ = steering
+        steering.register_plan(self.plan, getattr(self, "stream", None))
 
     def execute_pipeline(self, packet_data, dummy_run=False):
         raise NotImplementedError
@@ -131,6 +184,8 @@ class _Base(GPUPipeline):
 
     def _ingest(self, packet_data):
         import torch
+        if self.steering_ is not None:
+            self.steering_.maybe_refresh()  # first, as the reference's execute_pipeline
         with torch.cuda.stream(self.stream):
             s = torch.as_tensor(np.ascontiguousarray(packet_data.samples)).view(torch.int8)
             sc = torch.as_tensor(np.ascontiguousarray(packet_data.scales)).view(torch.int16)

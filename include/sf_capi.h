@@ -128,6 +128,21 @@ int sf_set_stream_permutation(sf_plan *plan, const int32_t *h_recv_perm, const i
 /* Beam weights, BeamWeightsT<T> payload (reference include/spatial/pipeline/common.hpp:52-55). */
 int sf_set_weights(sf_plan *plan, const uint16_t *h_weights_f16, void *stream);
 
+/* Steering-weight synthesis on the device, replacing compute_steering_weights and the weight copy of
+ * BeamSteering::maybe_refresh (reference include/spatial/pipeline/common.hpp:97-185, 255-300): sets the
+ * plan's weights (the payload sf_set_weights sets) to
+ *   w[c][pol][b][r] = (1/R) G[c][pol][r] exp(i phase),  phase = -2 pi f_c / c_light (l e + m n + n u),
+ *   f_c = base_freq_hz + (min_freq_ch + c) channel_bw_hz,
+ * in double precision, rounded to float and then fp16 (as the reference); null inputs get exactly 0.
+ *   h_dircos     double [B][3]        direction cosines (l, m, n) of each beam's target, local ENU frame
+ *   h_enu        double [R][3]        position (east, north, up; metres) of each receiver's antenna
+ *   h_connected  int32  [R]           0 = null input (no antenna on the stream); NULL = all connected
+ *   h_cal_gains  float  [C][Pol][R][2] calibration gains G, or NULL for 1
+ * Blocks until the weights are written; the host arrays are free on return. */
+int sf_set_steering_weights(sf_plan *plan, const double *h_dircos, const double *h_enu, const int32_t *h_connected,
+                            double base_freq_hz, double channel_bw_hz, int32_t min_freq_ch, const float *h_cal_gains,
+                            void *stream);
+
 /* Fixed K per channel (the -e map of the adaptive pipeline,
  * lambda_adaptive_beamformed_spectra_pipeline.hpp:1160-1167); NULL resets to 0. */
 int sf_set_fixed_counts(sf_plan *plan, const int32_t *h_counts, void *stream);

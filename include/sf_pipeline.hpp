@@ -48,7 +48,12 @@
  * Output::register_fft_block / get_fft_landing_pointer /
  * register_fft_transfer_complete.  Shapes the spectra kernels do not cover
  * (T not a power of two in [64, 16384]; Tp not 16, 32 or 64) skip the tail and
- * register no FFT block.  Beam steering is not part of this path.
+ * register no FFT block.
+ *
+ * Beam steering: set_beam_steering(SfBeamSteering<Config>) (sf_pointing.hpp)
+ * registers every buffer's plan; execute_pipeline then calls maybe_refresh()
+ * first, before any work of the run is enqueued, as the reference's pipelines
+ * do with their BeamSteering (lambda_gpu_pipeline.hpp:454-456, 973).
  */
 #ifndef SF_PIPELINE_HPP
 #define SF_PIPELINE_HPP
@@ -67,6 +72,7 @@
 #include <vector>
 
 #include "sf_capi.h"
+#include "sf_pointing.hpp"
 
 namespace sfgb {
 
@@ -245,9 +251,16 @@ template <typename Config, typename Base, int Mode> class SfPipelineBase : publi
       detail::check(sf_set_stream_permutation(b->plan, rp.data(), pp.data(), b->stream), "sf_set_stream_permutation");
   }
 
+  // Keep the beams pointed at the steering's targets (inert without targets).
+  void set_beam_steering(SfBeamSteering<Config> steering) {
+    steering_ = std::move(steering);
+    for (auto &b : buffers_) steering_.register_plan(b->plan, b->stream);
+  }
+
   void execute_pipeline(FinalPacketData *packet_data, const bool dummy_run = false) override {
     if (!dummy_run && this->state_ == nullptr)
       throw std::logic_error("State has not been set on GPUPipeline object!");
+    steering_.maybe_refresh();
     Buffer &b = *buffers_[current_];
     if (packet_data->get_samples_elements_size() != b.samples.bytes() ||
         packet_data->get_scales_element_size() != b.scales.bytes())
@@ -407,6 +420,7 @@ template <typename Config, typename Base, int Mode> class SfPipelineBase : publi
   }
 
   std::vector<std::unique_ptr<Buffer>> buffers_;
+  SfBeamSteering<Config> steering_;
   detail::DeviceArray<int64_t> accum_;
   detail::DeviceArray<float> vis_f32_;
   cudaEvent_t last_accumulate_ = nullptr;

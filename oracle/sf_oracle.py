@@ -373,6 +373,36 @@ def shrink_projection(v, evals, k):
     return (v * d[None, :]) @ np.conj(v.T)
 
 
+SPEED_OF_LIGHT = 299792458.0
+
+
+def steering_weights(shape, dircos, enu, connected=None, base_freq_hz=0.0, channel_bw_hz=0.0,
+                     min_freq_ch=0, cal_gains=None):
+    """compute_steering_weights (include/spatial/pipeline/common.hpp:97-185) as
+    fp16 pairs [C][Pol][B][R][2]: w = (1/R) G exp(i phase),
+    phase = -2 pi f_c / c (l e + m n + n u), f_c = base + (min_ch + c) bw, in
+    float64, rounded to float32 and then fp16; null inputs (connected == 0)
+    exactly zero.  dircos [B][3], enu [R][3], cal_gains complex [C][Pol][R]."""
+    C, B, R = shape.C, shape.B, shape.R
+    dc = np.asarray(dircos, dtype=np.float64).reshape(B, 3)
+    pos = np.asarray(enu, dtype=np.float64).reshape(R, 3)
+    path = (dc[:, 0, None] * pos[None, :, 0] + dc[:, 1, None] * pos[None, :, 1]) + dc[:, 2, None] * pos[None, :, 2]
+    f = base_freq_hz + (min_freq_ch + np.arange(C)).astype(np.float64) * channel_bw_hz
+    phase = (-2.0 * np.pi * f / SPEED_OF_LIGHT)[:, None, None] * path[None]  # [C][B][R]
+    ph = np.cos(phase) + 1j * np.sin(phase)
+    if cal_gains is None:
+        g = np.ones((C, NPOL, R), dtype=np.complex128)
+    else:
+        g = np.asarray(cal_gains).reshape(C, NPOL, R).astype(np.complex64).astype(np.complex128)
+    w = ((1.0 / R) * g)[:, :, None, :] * ph[:, None, :, :]  # [C][Pol][B][R]
+    if connected is not None:  # null inputs stay at the zero the result was initialised with
+        w = np.where((np.asarray(connected).reshape(R) != 0)[None, None, None, :], w, 0.0)
+    out = np.empty(w.shape + (2,), dtype=np.float16)
+    out[..., 0] = w.real.astype(np.float32).astype(np.float16)
+    out[..., 1] = w.imag.astype(np.float32).astype(np.float16)
+    return out
+
+
 def weights_complex(weights):
     """BeamWeightsT layout complex<__half>[C][Pol][B][R] (pipeline/common.hpp:52-55)
     given as float pairs [..., 2] or complex."""

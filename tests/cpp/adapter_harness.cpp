@@ -7,7 +7,10 @@
 // (include/spatial/pipeline_base.hpp:9-40, packet_formats.hpp:50-66,
 // output.hpp:22-58, spatial.hpp:149-247).
 //
-// usage: adapter_harness <mode 0|1|2> <dir>
+// usage: adapter_harness <mode 0|1|2> <dir> [steer]
+//   steer: attach an SfBeamSteering (zenith targets; receiver r at antenna 200 + r,
+//          ENU (3 r, -2 r, 0.5 r + r % 3); receiver 4 a null input; 1.0 GHz + ch x 100 kHz
+//          from channel 50) before the first run
 //   reads  dir/samples.bin (int8, two integrations), dir/scales.bin (int16, two),
 //          dir/weights.bin (fp16 pairs)
 //   writes dir/beams_<run>.bin, dir/vis.bin (float, after one dump of both runs),
@@ -245,14 +248,33 @@ int main(int argc, char **argv) {
 
     std::unique_ptr<GPUPipeline> pipeline;
     int delays[Cfg::NR_FPGA_SOURCES] = {3, -5};
+    const bool steer = argc > 3 && std::string(argv[3]) == "steer";
+    sfgb::SfBeamSteering<Cfg> steering;
+    if (steer) {
+      std::unordered_map<int, sfgb::ENUPosition> positions;
+      std::unordered_map<int, int> mapping;
+      for (int r = 0; r < R; ++r) {
+        positions[200 + r] = sfgb::ENUPosition{3.0 * r, -2.0 * r, 0.5 * r + r % 3};
+        mapping[r] = r == 4 ? -100 : 200 + r;
+      }
+      steering = sfgb::SfBeamSteering<Cfg>({sfgb::BeamTarget{}}, positions, mapping,
+                                           sfgb::FrequencyPlan{1.0e9, 1.0e5}, 50,
+                                           sfgb::ArrayLocation{52.9, 6.87, 30.0}, 1.0e6);
+    }
     if (mode == 0) {
-      pipeline.reset(new sfgb::SfLambdaCorrBeamOnlyGPUPipeline<Cfg>(2, weights.get(), 2));
+      auto *p = new sfgb::SfLambdaCorrBeamOnlyGPUPipeline<Cfg>(2, weights.get(), 2);
+      if (steer) p->set_beam_steering(steering);
+      pipeline.reset(p);
     } else if (mode == 1) {
-      pipeline.reset(new sfgb::SfLambdaGPUPipeline<Cfg>(2, weights.get(), 2));
+      auto *p = new sfgb::SfLambdaGPUPipeline<Cfg>(2, weights.get(), 2);
+      if (steer) p->set_beam_steering(steering);
+      pipeline.reset(p);
     } else {
       std::unordered_map<int, int> k_map;
       for (int c = 0; c < C; ++c) k_map[100 + c] = c % 3;  // absolute channel -> K
-      pipeline.reset(new sfgb::SfLambdaAdaptivePipeline<Cfg>(2, weights.get(), k_map, 100, false, false, 3.0f, 2));
+      auto *p = new sfgb::SfLambdaAdaptivePipeline<Cfg>(2, weights.get(), k_map, 100, false, false, 3.0f, 2);
+      if (steer) p->set_beam_steering(steering);
+      pipeline.reset(p);
     }
     pipeline->set_state(&state);
     pipeline->set_output(output);

@@ -47,12 +47,13 @@ def inputs():
     return sh, [s0, s1], [sc0, sc1], w
 
 
-def _run(harness, mode, inputs, tmp_path):
+def _run(harness, mode, inputs, tmp_path, steer=False):
     sh, samples, scales, w = inputs
     np.concatenate([s.reshape(-1) for s in samples]).astype(np.int8).tofile(tmp_path / "samples.bin")
     np.concatenate([s.reshape(-1) for s in scales]).astype(np.int16).tofile(tmp_path / "scales.bin")
     np.ascontiguousarray(w).tofile(tmp_path / "weights.bin")
-    res = subprocess.run([harness, str(mode), str(tmp_path)], capture_output=True, text=True, timeout=300)
+    cmd = [harness, str(mode), str(tmp_path)] + (["steer"] if steer else [])
+    res = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
     assert res.returncode == 0, res.stderr
     proto = {}
     for line in (tmp_path / "protocol.txt").read_text().splitlines():
@@ -65,11 +66,18 @@ def _dev(x, dtype):
     return torch.as_tensor(np.ascontiguousarray(x)).to(device="cuda").view(dtype)
 
 
-def _direct(mode, inputs):
+# the harness's steering geometry (adapter_harness.cpp, "steer")
+STEER_ENU = [(3.0 * r, -2.0 * r, 0.5 * r + r % 3) for r in range(R)]
+STEER_CONNECTED = [0 if r == 4 else 1 for r in range(R)]
+
+
+def _direct(mode, inputs, steer=False):
     """The same two integrations through the C ABI directly."""
     sh, samples, scales, w = inputs
     plan = sfgb.Plan(C, F, TP, R, RPP, P, B)
     plan.set_weights(w)
+    if steer:
+        plan.set_steering_weights([(0.0, 0.0, 1.0)] * B, STEER_ENU, STEER_CONNECTED, 1.0e9, 1.0e5, 50)
     if mode != 0:
         plan.set_subpacket_delays(DELAYS)
     if mode == 2:
@@ -175,3 +183,18 @@ def test_adapter_visibilities_match_oracle(harness, inputs, tmp_path):
         total = v if total is None else total + v
     vis = np.fromfile(tmp_path / "vis.bin", dtype=np.float32).reshape(total.shape)
     assert np.array_equal(vis.astype(np.int64), total)
+
+
+@pytest.mark.parametrize("mode", [0, 2], ids=["corr_beam_only", "adaptive"])
+def test_adapter_beam_steering(harness, inputs, tmp_path, mode):
+    """An attached SfBeamSteering refreshes the plans' weights before the first
+    run: the landed beams equal a direct chain whose plan was steered with the
+    same geometry, and differ from the unsteered ones."""
+    _run(harness, mode, inputs, tmp_path, steer=True)
+    ref = _direct(mode, inputs, steer=True)
+    plain = _direct(mode, inputs)
+    slots = 2 if mode == 2 else 1
+    for run in range(2):
+        got = np.fromfile(tmp_path / f"beams_{run}.bin", dtype=np.float16).reshape(C, 2, slots * B, P * TP, 2)
+        assert np.array_equal(got, ref["beams"][run])
+        assert not np.array_equal(got, plain["beams"][run])
