@@ -67,7 +67,8 @@ constexpr int NUM_WORKERS = NUM_CONV_WARPS - 1;  // warps that convert
 constexpr uint32_t BAR_START = 1, BAR_END = 2;  // named barriers of the converter group
 constexpr int MAX_SLOTS = 32;
 constexpr int MAX_F = 64;
-constexpr uint32_t HEADER_BYTES = 2048;
+constexpr uint32_t HEADER_BYTES = 3072;
+constexpr int MAX_ITEMS = 64;  // work items of one CTA (whole channels + tail pieces)
 constexpr int MAX_R = 48;
 constexpr int MAX_BEAM_OUT = 16;  // beams (all slots) per pol in the tensor beamformer
 // receiver pairs (16-byte chunks of a sample) one converter warp owns at most
@@ -120,8 +121,51 @@ struct __align__(8) Header {
   int rx_woff[MAX_R];  // window offset (samples) of receiver r's FPGA
   uint32_t unit_bits[2];  // per stage parity: bit s = ring slot s holds a packet whose scales are all 1
   int perm[2 * MAX_R];    // output stream 2 r + p <- source (src_r << 1) | src_pol, -1 = zero
+  int n_items;
+  int4 items[MAX_ITEMS];  // channel, first stage, end stage, whole (stored) or piece (atomics)
 };
 static_assert(sizeof(Header) <= HEADER_BYTES, "header too large");
+
+// The work of one CTA: channels [0, full_end) are processed whole, C / G of
+// them per CTA (channel b, b + G, ...); the stages of the remaining channels
+// are concatenated and dealt out as one contiguous range per CTA, cut at
+// channel boundaries into pieces.  Every CTA then carries the same number of
+// stages to within one, instead of whole channels to within one (384 channels
+// on 152 SMs: 2.53 channels each, not 3).  Pieces of a channel on different
+// CTAs add their exact int32 partial visibilities with integer atomics into a
+// region the launcher zeroes; whole channels store them.  Every role walks
+// the same list in the same order.
+struct WorkItems {
+  int nst, G, b, full, full_end;
+  int t, t1;  // cursor and end of this CTA's range of tail stages (32-bit: C * nst < 2^31)
+  int i;      // whole channels handed out so far
+  __device__ __forceinline__ WorkItems(int C, int nst_) : nst(nst_), G(gridDim.x), b(blockIdx.x), i(0) {
+    full = C / G;
+    full_end = full * G;
+    const int ts = (C - full_end) * nst;  // < G * nst
+    t = static_cast<int>((static_cast<unsigned>(ts) * static_cast<unsigned>(b)) / static_cast<unsigned>(G));
+    t1 = static_cast<int>((static_cast<unsigned>(ts) * static_cast<unsigned>(b + 1)) / static_cast<unsigned>(G));
+  }
+  // Next item: channel c, stages [pb, pe); whole = stored, else atomically added.
+  __device__ __forceinline__ bool next(int &c, int &pb, int &pe, bool &whole) {
+    if (i < full) {
+      c = b + i * G;
+      ++i;
+      pb = 0;
+      pe = nst;
+      whole = true;
+      return true;
+    }
+    if (t >= t1) return false;
+    const int tc = t / nst;
+    c = full_end + tc;
+    pb = t - tc * nst;
+    pe = min(nst, pb + (t1 - t));
+    t += pe - pb;
+    whole = false;
+    return true;
+  }
+};
 
 __device__ __forceinline__ uint32_t u32_of(__half2 h) { return *reinterpret_cast<uint32_t *>(&h); }
 __device__ __forceinline__ __half2 h2_of(uint32_t u) { return *reinterpret_cast<__half2 *>(&u); }
@@ -157,9 +201,10 @@ __device__ __forceinline__ void convert_word(uint32_t word, uint32_t scw, __half
 }
 
 __device__ __forceinline__ void emit_vis(const CorrArgs &a, int c, int p, int i, int q, int j,
-                                         int comp, int val) {
+                                         int comp, int val, bool whole) {
   const size_t idx = ((((size_t)c * a.NBL + baseline_of(i, j)) * 2 + p) * 2 + q) * 2 + comp;
-  a.vis[idx] = val;
+  if (whole) a.vis[idx] = val;
+  else atomicAdd(a.vis + idx, val);  // exact: integer addition in any order
 }
 
 // Shared-memory descriptor with explicit strides (128-byte swizzle).  K-major:
@@ -219,6 +264,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     h.abort = 0;
     fence_mbarrier_init();
   }
+  if (tid == 0) {
+    WorkItems wi(a.C, a.nkb >> 1);
+    int c, pb, pe, n = 0;
+    bool whole;
+    while (n < MAX_ITEMS && wi.next(c, pb, pe, whole)) h.items[n++] = make_int4(c, pb, pe, whole ? 1 : 0);
+    h.n_items = n;  // the host keeps C / G + 2 <= MAX_ITEMS
+  }
   for (int f = tid; f < a.F; f += NTHREADS) h.offsets[f] = a.offsets[f];
   for (int k = tid; k < 2 * a.R; k += NTHREADS) h.perm[k] = a.perm ? a.perm[k] : ((k >> 1) << 1) | (k & 1);
   for (int r = tid; r < a.R; r += NTHREADS) {
@@ -248,21 +300,23 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     off_max = max(off_max, h.offsets[f]);
   }
   const int Tp = a.Tp, T = a.T, R = a.R;
-  const int qa0 = off_min / Tp;
-  const int qbN = min(a.P + 1, (T - 1 + off_max) / Tp);
-  const int npk = qbN - qa0 + 1;
-  const int nchunks = (a.nkb + CHUNK_KBLK - 1) / CHUNK_KBLK;
-  const int npairs = a.nkb >> 1;
+  const int npairs = a.nkb >> 1;  // stages per channel
+  // packets stages [pb, pe) read: [q_lo(pb), q_hi(pe)]
+  auto q_lo = [&](int pb) { return (pb * TILE_T + off_min) / Tp; };
+  auto q_hi = [&](int pe) { return min(a.P + 1, (min(pe * TILE_T, T) - 1 + off_max) / Tp); };
   volatile int *abort_flag = &h.abort;
 
   if (warp == WARP_TMA) {
     // ---------------- producer (whole warp) ----------------
     uint32_t g = 0;
     bool stop = false;
-    for (int c = blockIdx.x; c < a.C && !stop; c += gridDim.x) {
+    for (int it = 0; it < h.n_items && !stop; ++it) {
+      const int4 w = h.items[it];
+      const int c = w.x, pb = w.y, pe = w.z;
       const int8_t *chan = a.samples + (size_t)c * (a.P + 2) * a.slot_bytes;
       const int16_t *chan_sc = a.scales + (size_t)c * (a.P + 2) * R * 2;
-      for (int q = qa0; q <= qbN; ++q) {
+      const int qend = q_hi(pe);
+      for (int q = q_lo(pb); q <= qend; ++q) {
         const uint32_t slot = g & ns_mask;
         const bool ok = mbar_wait(&h.pk_empty[slot], ((g >> ns_shift) & 1u) ^ 1u, abort_flag, 20000);
         if (__any_sync(0xffffffffu, !ok)) {
@@ -307,20 +361,22 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
       const uint64_t d_w0 = desc_sw128(w_addr, 16, 1024);
       uint32_t op_iter = 0, acc_iter = 0, beam_iter = 0, cw = 0;
       bool failed = false;
-      for (int c = blockIdx.x; c < a.C; c += gridDim.x, ++cw) {
+      for (int it = 0; it < h.n_items; ++it, ++cw) {
+        const int pb = h.items[it].y, pe = h.items[it].z;
         const uint32_t wb = cw & 1u;
         if (DO_BEAM) failed |= !mbar_wait(&h.w_full[wb], (cw >> 1) & 1u, abort_flag, SUSPEND_NS);
         const uint32_t woff = wb * a.wtile_bytes;
-        for (int pr = 0; pr < npairs; ++pr) {
+        for (int pr = pb; pr < pe; ++pr) {
           const uint32_t st = op_iter & 1u;
           bool ok = mbar_wait(&h.op_full[st], (op_iter >> 1) & 1u, abort_flag, SUSPEND_NS);
           tc_fence_after();
           const uint32_t soff = st * stage_bytes;
           if (DO_CORR) {
-            // a chunk (CHUNK_KBLK K blocks) starts and ends on stage boundaries
-            const int kb0 = 2 * pr;
+            // a chunk (CHUNK_KBLK K blocks from the item's first stage) starts
+            // and ends on stage boundaries
+            const int kb0 = 2 * (pr - pb);
             const bool chunk_start = (kb0 % CHUNK_KBLK) == 0;
-            const bool chunk_end = ((kb0 + 1) % CHUNK_KBLK) == CHUNK_KBLK - 1 || kb0 + 1 == a.nkb - 1;
+            const bool chunk_end = ((kb0 + 1) % CHUNK_KBLK) == CHUNK_KBLK - 1 || pr == pe - 1;
             const uint32_t abuf = acc_iter % a.nacc;
             if (chunk_start) {
               ok = mbar_wait(&h.acc_empty[abuf], ((acc_iter / a.nacc) & 1u) ^ 1u, abort_flag, SUSPEND_NS) && ok;
@@ -382,8 +438,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     const int ncplx = 2 * a.NB;  // beam output columns (pol, beam)
     uint32_t acc_iter = 0, beam_iter = 0;
     bool failed = false;
-    for (int c = blockIdx.x; c < a.C; c += gridDim.x) {
-      for (int kb = 0; kb < a.nkb; ++kb) {
+    for (int it = 0; it < h.n_items; ++it) {
+      const int4 w = h.items[it];
+      const int c = w.x, pb = w.y, pe = w.z;
+      for (int kb = 2 * pb; kb < 2 * pe; ++kb) {
         if (DO_BEAM && (kb & 1)) {
           const uint32_t buf = beam_iter & 1u;
           const bool ok = mbar_wait(&h.beam_full[buf], (beam_iter >> 1) & 1u, abort_flag, 20000);
@@ -418,14 +476,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
           }
           ++beam_iter;
         }
-        if (!DO_CORR || !((kb % CHUNK_KBLK) == CHUNK_KBLK - 1 || kb == a.nkb - 1)) continue;
-        const int ch = kb / CHUNK_KBLK;
+        if (!DO_CORR || !(((kb - 2 * pb) % CHUNK_KBLK) == CHUNK_KBLK - 1 || kb == 2 * pe - 1)) continue;
+
         const uint32_t abuf = acc_iter % a.nacc;
         const bool ok = mbar_wait(&h.acc_full[abuf], (acc_iter / a.nacc) & 1u, abort_flag, 20000);
         failed |= !ok;
         tc_fence_after();
-        const bool first = ch == 0;
-        const bool last = ch == nchunks - 1;
+        const bool first = kb - 2 * pb < CHUNK_KBLK;  // the item's first chunk
+        const bool last = kb == 2 * pe - 1;           // the item's last chunk
         const uint32_t tacc = tmem + abuf * a.acc_stride;
         for (int cb = 0; cb < ncols / 16; ++cb) {
           uint32_t fv[16], sv[16];
@@ -453,6 +511,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
           const int i = k >> 1;
           const bool row_ok = ok && u < R4;
           const int m0 = main_region ? cb * 8 : 64 + ((cb * 16 - NR) >> 1);
+          const bool whole = *reinterpret_cast<volatile int *>(&h.items[it].w) != 0;
 #pragma unroll
           for (int e2 = 0; e2 < 8; ++e2) {
             const int g0 = acc[2 * e2];
@@ -463,10 +522,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
             if (!row_ok || 2 * m >= R4) continue;
             const int q = m & 1;
             const int j = m >> 1;
-            if (i <= j) emit_vis(a, c, p, i, q, j, comp, val);
+            if (i <= j) emit_vis(a, c, p, i, q, j, comp, val, whole);
             // Rows m >= 64 are not main-tile rows: their entries with a main-tile
             // column come from here, conjugated.
-            if (main_region && m >= 64 && j <= i) emit_vis(a, c, q, j, p, i, comp, comp ? -val : val);
+            if (main_region && m >= 64 && j <= i) emit_vis(a, c, q, j, p, i, comp, comp ? -val : val, whole);
           }
         }
         if (!last) tmem_wait_st();
@@ -522,7 +581,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     // free operand stage for op_iter_next; publish the packet flags
     auto acquire = [&](int pr, uint32_t gq0, uint32_t it) {
       const int s0 = pr * TILE_T;
-      const int qb = s0 < T ? min(a.P + 1, (min(s0 + TILE_T - 1, T - 1) + off_max) / Tp) : qbN;
+      const int qb = s0 < T ? min(a.P + 1, (min(s0 + TILE_T - 1, T - 1) + off_max) / Tp) : q_hi(npairs);
       bool ok = true;
       for (; q_wait <= qb && ok; ++q_wait) {
         const uint32_t gq = gq0 + q_wait;
@@ -541,7 +600,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
       }
       return ok;
     };
-    for (int c = blockIdx.x; c < a.C; c += gridDim.x, ++cw) {
+    for (int it = 0; it < h.n_items; ++it, ++cw) {
+      const int c = h.items[it].x, pb = h.items[it].y, pe = h.items[it].z;
+      const int qlo = q_lo(pb), qhi = q_hi(pe);
       if (DO_BEAM) {
         // weight tile for this channel: B[n][u], n = (pol, beam, re/im),
         // u = (receiver, pol, re/im), K-major, 128-byte swizzle, one
@@ -584,25 +645,25 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
         __syncwarp();
         if (lane == 0) mbar_arrive(&h.w_full[wb]);
       }
-      const uint32_t gq0 = g_base - static_cast<uint32_t>(qa0);  // ring index of packet q: gq0 + q
+      const uint32_t gq0 = g_base - static_cast<uint32_t>(qlo);  // ring index of packet q: gq0 + q
       if (leader) {
-        q_rel = qa0;
-        q_wait = qa0;
-        acq_ok = acquire(0, gq0, op_iter);
+        q_rel = qlo;
+        q_wait = qlo;
+        acq_ok = acquire(pb, gq0, op_iter);
       }
-      for (int pr = 0; pr < npairs; ++pr) {
+      for (int pr = pb; pr < pe; ++pr) {
         const int s0 = pr * TILE_T;
         const uint32_t st = op_iter & 1u;
         named_bar_sync(BAR_START, NUM_CONV_THREADS);  // stage pr is open
         if (leader) {
           // the next stage's resources while the converters work
-          const bool more = pr + 1 < npairs;
+          const bool more = pr + 1 < pe;
           if (more && a.prefetch) acq_ok = acquire(pr + 1, gq0, op_iter + 1);
           named_bar_sync(BAR_END, NUM_CONV_THREADS);  // every converter is done with stage pr
           if (lane == 0) {
             mbar_arrive(&h.op_full[st]);
             // packets no later stage needs go back to the producer
-            int next = qbN + 1;
+            int next = qhi + 1;
             if (more && s0 + TILE_T < T) next = (s0 + TILE_T + off_min) / Tp;
             for (; q_rel < next; ++q_rel) mbar_arrive(&h.pk_empty[(gq0 + q_rel) & ns_mask]);
           }
@@ -710,7 +771,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
         }
         ++op_iter;
       }
-      g_base += npk;
+      g_base += qhi - qlo + 1;
     }
     (void)acq_ok;
     if (failed && lane == 0) atomicOr(a.status, SF_DEVERR_TIMEOUT_CONVERT);
@@ -844,6 +905,19 @@ cudaError_t sf_launch_corrbeam(const sf_plan *p, const int8_t *samples, const in
   a.prefetch = ns >= (2 * TILE_T - 1) / p->Tp + 5 ? 1 : 0;
   const size_t smem = fixed + (size_t)ns * a.slot_stride;
   const int grid = std::max(1, std::min(p->C, p->num_sms));
+  // WorkItems computes (tail stages) x (CTA index) in 32 bits; a CTA holds at
+  // most C / grid whole channels and two pieces
+  if ((double)(p->C % grid) * (a.nkb / 2) * grid >= 4294967296.0) return cudaErrorInvalidConfiguration;
+  if (p->C / grid + 2 > MAX_ITEMS) return cudaErrorInvalidConfiguration;
+  if (do_corr) {
+    // channels past the whole-channel share are summed from pieces by integer atomics
+    const int full_end = (p->C / grid) * grid;
+    if (full_end < p->C) {
+      const size_t per = (size_t)p->NBL * 8;
+      cudaError_t e = cudaMemsetAsync(vis + (size_t)full_end * per, 0, sizeof(int32_t) * (p->C - full_end) * per, stream);
+      if (e != cudaSuccess) return e;
+    }
+  }
   if (do_corr && do_beam) return launch_corner<true, true>(a, smem, grid, stream);
   if (do_corr) return launch_corner<true, false>(a, smem, grid, stream);
   return launch_corner<false, true>(a, smem, grid, stream);

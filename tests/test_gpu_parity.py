@@ -473,3 +473,80 @@ def test_stream_permutation_rejects_bad_tables():
     pipe.set_stream_permutation(list(good_r), list(good_p))  # identity table is accepted
     pipe.plan.close()
     plan.close()
+
+
+# --------------------------------------------------------------------------
+# Balanced work split: with more channels than SMs, the channels past the
+# whole-channel share are cut into stage ranges spread over every CTA; their
+# partial visibilities are added with integer atomics.  160 channels of 1024
+# samples: 8 tail channels, each cut across many CTAs.
+# --------------------------------------------------------------------------
+@pytest.fixture(scope="module")
+def split_case():
+    sh = orc.Shape(160, 4, 64, 36, 9, 16, 4)
+    samples, scales, _ = orc.synth_inputs(sh, seed=31, n_interferers=2, frac_channels=0.5)
+    weights = orc.synth_weights(sh, seed=32)
+    return sh, samples, scales, weights
+
+
+def test_correlator_split_channels_scaled_packets():
+    """Pieces with non-unit packet scales (the general conversion path).
+    Amplitudes stay where every 1024-sample fp32 Gram partial is an exact
+    integer (|x s| <= 96: 1024 x 96^2 < 2^24), so the result is bit-exact."""
+    import os
+    import sf_oracle_c as sfc
+    sh = orc.Shape(160, 4, 64, 36, 9, 16, 1)
+    rng = np.random.default_rng(34)
+    samples = rng.integers(-32, 33, size=sh.samples_shape()).astype(np.int8)
+    scales = np.where(rng.random(sh.scales_shape()) < 0.3, rng.integers(2, 4, size=sh.scales_shape()), 1).astype(np.int16)
+    delays = [3, -9, 0, 40]
+    got = _correlate_gpu(sh, samples, scales, sfgb.SF_WINDOW_ALIGNED, delays)
+    ref = sfc.correlate(sh, samples, scales, orc.sample_offsets(sh, delays), nthreads=os.cpu_count())
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("window,delays", [(sfgb.SF_WINDOW_ALIGNED, [0, 5, -7, 64]),
+                                           (sfgb.SF_WINDOW_PACKET, None)])
+def test_correlator_split_channels_bit_exact(split_case, window, delays):
+    import os
+    import sf_oracle_c as sfc
+    sh, samples, scales, _ = split_case
+    got = _correlate_gpu(sh, samples, scales, window, delays)
+    mode = "aligned" if window == sfgb.SF_WINDOW_ALIGNED else "packet"
+    ref = sfc.correlate(sh, samples, scales, orc.sample_offsets(sh, delays, mode=mode), nthreads=os.cpu_count())
+    assert np.array_equal(got, ref)
+
+
+def _beam_close(got, ref_beams, B):
+    yb = got[..., 0] + 1j * got[..., 1]
+    err = np.abs(yb - ref_beams)
+    scale = np.abs(ref_beams).max(axis=-1, keepdims=True)
+    bound = 2.0 ** -9 * np.abs(ref_beams) + 2.0 ** -6 + 2e-3 * scale
+    assert np.all(err[:, :, :B] <= bound[:, :, :B])
+    assert np.all(err <= bound)
+
+
+def test_adaptive_chain_split_channels(split_case):
+    sh, samples, scales, weights = split_case
+    fixed = np.full(sh.C, 2)
+    got = _run_adaptive_gpu(sh, samples, scales, weights, sfgb.SF_K_FIXED, 0.0, fixed=fixed, want_evecs=False)
+    ref = orc.adaptive_chain(sh, samples, scales, weights, k_fixed=fixed)
+    assert np.array_equal(got["vis"], ref["vis"])
+    _beam_close(got["beams"], ref["beams"], sh.B)
+
+
+def test_corr_beam_fused_split_channels(split_case):
+    sh, samples, scales, weights = split_case
+    plan = sfgb.Plan(sh.C, sh.F, sh.Tp, sh.R, sh.Rpp, sh.P, sh.B)
+    plan.set_weights(weights)
+    s, sc = _dev(samples, torch.int8), _dev(scales, torch.int16)
+    vis = torch.full(plan.vis_shape(), -7, dtype=torch.int32, device="cuda")
+    beams = torch.empty(plan.beams_shape(1), dtype=torch.float16, device="cuda")
+    plan.run_corr_beam(s, sc, vis, beams)
+    torch.cuda.synchronize()
+    rc, bits = plan.status()
+    assert rc == 0 and bits == 0
+    plan.close()
+    ref = orc.corr_beam_chain(sh, samples, scales, weights)
+    assert np.array_equal(vis.cpu().numpy(), ref["vis"])
+    _beam_close(beams.cpu().numpy().astype(np.float32), ref["beams"], sh.B)
