@@ -1,8 +1,10 @@
 // Tensor-core correlator and beamformer over one integration of int8 complex
 // voltages in the packet layout.
 //
-// One persistent CTA per SM streams each channel's packets once through
-// shared memory and builds, per 128 samples, one fp16 operand tile
+// One persistent CTA per SM streams its channels' packets once through
+// shared memory (whole channels, then a balanced range of the remaining
+// channels' stages; see WorkItems) and builds, per 128 samples, one fp16
+// operand tile
 //   X[t][u],  u = 4 r + 2 pol + comp   (receiver r, polarization, re/im)
 // i.e. the packet's own byte order: for every sample the 4R values of the
 // channel are contiguous.  The tile is stored as 64-value atoms
