@@ -50,9 +50,9 @@ struct TopkArgs {
 };
 
 __host__ __device__ inline size_t topk_floats(int n, int B) {
-  // float2: A (n x (n+1)), 2 v, p, tau, Z (NW x n), Wp (B x n), coef (NW x B)
+  // float2: A (n x (n+1)), 2 v, p, tau, Z (NW x n), Wp (B x n), W0 (B x n), coef (NW x B)
   // float:  X (n x n), LU workspace (5 GROUP x n), d, e, e2, lam, sd
-  const size_t f2 = (size_t)n * (n + 1) + 4 * (size_t)n + (size_t)NW * n + (size_t)B * n + (size_t)NW * B;
+  const size_t f2 = (size_t)n * (n + 1) + 4 * (size_t)n + (size_t)NW * n + 2 * (size_t)B * n + (size_t)NW * B;
   const size_t f = (size_t)n * n + 5 * (size_t)GROUP * n + 5 * (size_t)n;
   return ((2 * f2 + f) + 3) & ~(size_t)3;
 }
@@ -150,7 +150,7 @@ __device__ __forceinline__ void make_reflector(float2 *A, int ld, int n, int k, 
   }
 }
 
-__global__ void __launch_bounds__(NT) sf_eig_topk_kernel(const TopkArgs a) {
+__global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ float s_red[4 * NW];
   __shared__ float s_scal[8];
@@ -170,7 +170,8 @@ __global__ void __launch_bounds__(NT) sf_eig_topk_kernel(const TopkArgs a) {
   float2 *taus = pb + n;                         // reflector scalars
   float2 *Z = taus + n;                          // NW back-transformed vectors
   float2 *Wp = Z + NW * n;                       // projected weights B x n
-  float2 *coef = Wp + B * n;                     // NW x B projection coefficients
+  float2 *W0 = Wp + B * n;                       // the original weights B x n
+  float2 *coef = W0 + B * n;                     // NW x B projection coefficients
   float *X = reinterpret_cast<float *>(coef + NW * B);  // top-K vectors of T, K x n
   float *U0 = X + n * n;                         // LU workspace, GROUP x n each
   float *U1 = U0 + GROUP * n;
@@ -422,7 +423,7 @@ __global__ void __launch_bounds__(NT) sf_eig_topk_kernel(const TopkArgs a) {
           const float ns = (i + 1 < n - 1) ? e[i + 1] : 0.0f;
           if (fabsf(cd) >= fabsf(sub)) {
             const float piv = fabsf(cd) < pert ? (cd < 0.0f ? -pert : pert) : cd;
-            const float rp = 1.0f / piv;
+            const float rp = __frcp_rn(piv);
             const float l = sub * rp;
             u0[i] = rp;
             u1[i] = cs;
@@ -432,8 +433,9 @@ __global__ void __launch_bounds__(NT) sf_eig_topk_kernel(const TopkArgs a) {
             cd = nd - l * cs;
             cs = ns;
           } else {
-            const float l = cd / sub;
-            u0[i] = 1.0f / (fabsf(sub) < pert ? pert : sub);
+            const float rs = __frcp_rn(fabsf(sub) < pert ? pert : sub);
+            const float l = cd * rs;
+            u0[i] = rs;
             u1[i] = nd;
             u2[i] = ns;
             pv[i] = 1.0f;
@@ -442,9 +444,13 @@ __global__ void __launch_bounds__(NT) sf_eig_topk_kernel(const TopkArgs a) {
             cs = -l * ns;
           }
         }
-        u0[n - 1] = 1.0f / ((fabsf(cd) < pert) ? (cd < 0.0f ? -pert : pert) : cd);
+        u0[n - 1] = __frcp_rn((fabsf(cd) < pert) ? (cd < 0.0f ? -pert : pert) : cd);
         float *x = X + r * n;
-        for (int i = 0; i < n; ++i) x[i] = 1.0f + 0.37f * sinf(0.91f * (i + 1) * (r + 1));
+        // a fixed pseudo-random start in [0.5, 1.5): no eigenvector is orthogonal to it
+        for (int i = 0; i < n; ++i) {
+          const uint32_t hsh = (static_cast<uint32_t>(i + 1) * 2654435761u) ^ (static_cast<uint32_t>(r + 1) * 2246822519u);
+          x[i] = 0.5f + static_cast<float>((hsh >> 8) & 0xFFFFu) * (1.0f / 65536.0f);
+        }
       }
       for (int it = 0; it < INV_ITERS; ++it) {
         if (lane < gn) {
@@ -510,7 +516,11 @@ __global__ void __launch_bounds__(NT) sf_eig_topk_kernel(const TopkArgs a) {
 
   // ---- 6./7. back-transform (one warp per vector), projected weights ----
   const __half2 *w = a.weights + (size_t)bt * B * n;
-  for (int e0 = tid; e0 < B * n; e0 += NT) Wp[e0] = __half22float2(w[e0]);
+  for (int e0 = tid; e0 < B * n; e0 += NT) {
+    const float2 x = __half22float2(w[e0]);
+    Wp[e0] = x;
+    W0[e0] = x;
+  }
   float lam_bar = 0.0f;
   if (a.shrink && K < n) {
     for (int i = 0; i < n - K; ++i) lam_bar += lam[i];
@@ -521,29 +531,23 @@ __global__ void __launch_bounds__(NT) sf_eig_topk_kernel(const TopkArgs a) {
     const int r = g + warp;
     float2 *z = Z + warp * n;
     if (r < K) {
-      // z = Q x: apply the reflectors from the last to the first
+      // z = Q x: the reflectors from the last to the first, z in registers
+      // (lane holds elements lane and lane + 32, n <= 64); reflector k's v is 1
+      // at k + 1, A[j][k] below it, 0 above
       const float *x = X + r * n;
-      for (int i = lane; i < n; i += 32) z[i] = make_float2(x[i], 0.0f);
-      __syncwarp();
+      const int i0 = lane, i1 = lane + 32;
+      float2 z0 = make_float2(i0 < n ? x[i0] : 0.0f, 0.0f);
+      float2 z1 = make_float2(i1 < n ? x[i1] : 0.0f, 0.0f);
       for (int k = n - 2; k >= 0; --k) {
-        const int m = n - k - 1;
         const float2 tau = taus[k];
-        if (tau.x == 0.0f && tau.y == 0.0f) continue;
-        float dre = 0.0f, dim = 0.0f;
-        for (int i = lane; i < m; i += 32) {
-          const float2 v = i == 0 ? make_float2(1.0f, 0.0f) : A[(k + 1 + i) * ld + k];
-          const float2 t = cmulc(z[k + 1 + i], v);  // conj(v) z
-          dre += t.x;
-          dim += t.y;
-        }
+        const float2 v0 = i0 > k + 1 && i0 < n ? A[i0 * ld + k] : make_float2(i0 == k + 1 ? 1.0f : 0.0f, 0.0f);
+        const float2 v1 = i1 > k + 1 && i1 < n ? A[i1 * ld + k] : make_float2(i1 == k + 1 ? 1.0f : 0.0f, 0.0f);
+        float dre = v0.x * z0.x + v0.y * z0.y + v1.x * z1.x + v1.y * z1.y;  // conj(v) z
+        float dim = v0.x * z0.y - v0.y * z0.x + v1.x * z1.y - v1.y * z1.x;
         warp_sum2(dre, dim);
-        const float2 s = cmul(tau, make_float2(dre, dim));
-        for (int i = lane; i < m; i += 32) {
-          const float2 v = i == 0 ? make_float2(1.0f, 0.0f) : A[(k + 1 + i) * ld + k];
-          const float2 t = cmul(s, v);
-          z[k + 1 + i] = make_float2(z[k + 1 + i].x - t.x, z[k + 1 + i].y - t.y);
-        }
-        __syncwarp();
+        const float2 sc = cmul(tau, make_float2(dre, dim));
+        z0 = make_float2(z0.x - (sc.x * v0.x - sc.y * v0.y), z0.y - (sc.x * v0.y + sc.y * v0.x));
+        z1 = make_float2(z1.x - (sc.x * v1.x - sc.y * v1.y), z1.y - (sc.x * v1.y + sc.y * v1.x));
       }
       float wgt = 1.0f;
       if (a.shrink) {
@@ -551,30 +555,30 @@ __global__ void __launch_bounds__(NT) sf_eig_topk_kernel(const TopkArgs a) {
         wgt = 1.0f - (lk > 0.0f ? lam_bar / lk : 0.0f);
       } else {
         // un-whiten and normalise
-        float part = 0.0f;
-        for (int i = lane; i < n; i += 32) {
-          const float2 t = make_float2(z[i].x * sd[i], z[i].y * sd[i]);
-          z[i] = t;
-          part += t.x * t.x + t.y * t.y;
-        }
-        const float nrm2 = warp_sum(part);
+        const float s0 = i0 < n ? sd[i0] : 0.0f, s1 = i1 < n ? sd[i1] : 0.0f;
+        z0 = make_float2(z0.x * s0, z0.y * s0);
+        z1 = make_float2(z1.x * s1, z1.y * s1);
+        const float nrm2 = warp_sum(z0.x * z0.x + z0.y * z0.y + z1.x * z1.x + z1.y * z1.y);
         const float inv = nrm2 > 0.0f ? rsqrtf(nrm2) : 0.0f;
-        for (int i = lane; i < n; i += 32) z[i] = make_float2(z[i].x * inv, z[i].y * inv);
+        z0 = make_float2(z0.x * inv, z0.y * inv);
+        z1 = make_float2(z1.x * inv, z1.y * inv);
       }
-      __syncwarp();
-      // c_m = wgt (W_m . z): all partial sums first, then the reductions
+      if (i0 < n) z[i0] = z0;
+      if (i1 < n) z[i1] = z1;
+      // c_m = wgt (W_m . z) against the original weights: all partial sums
+      // first, then the reductions
       {
         float cre[MAX_B], cim[MAX_B];
 #pragma unroll
         for (int mm = 0; mm < MAX_B; ++mm) {
           cre[mm] = 0.0f;
           cim[mm] = 0.0f;
-          if (mm < B)
-            for (int i = lane; i < n; i += 32) {
-              const float2 t = cmul(__half22float2(w[mm * n + i]), z[i]);
-              cre[mm] += t.x;
-              cim[mm] += t.y;
-            }
+          if (mm < B) {
+            const float2 wa = i0 < n ? W0[mm * n + i0] : make_float2(0.0f, 0.0f);
+            const float2 wb = i1 < n ? W0[mm * n + i1] : make_float2(0.0f, 0.0f);
+            cre[mm] = wa.x * z0.x - wa.y * z0.y + wb.x * z1.x - wb.y * z1.y;
+            cim[mm] = wa.x * z0.y + wa.y * z0.x + wb.x * z1.y + wb.y * z1.x;
+          }
         }
 #pragma unroll
         for (int mm = 0; mm < MAX_B; ++mm) {
@@ -603,7 +607,7 @@ __global__ void __launch_bounds__(NT) sf_eig_topk_kernel(const TopkArgs a) {
   float2 *we = a.weff + (size_t)bt * 2 * B * n;
   for (int e0 = tid; e0 < B * n; e0 += NT) {
     const int col = e0 - (e0 / n) * n;
-    we[e0] = cmul(__half22float2(w[e0]), dp[col]);
+    we[e0] = cmul(W0[e0], dp[col]);
     we[B * n + e0] = cmul(Wp[e0], dp[col]);
   }
 }
