@@ -129,11 +129,11 @@ __device__ __forceinline__ void make_reflector(float2 *A, int ld, int n, int k, 
   if (!(xnorm2 == 0.0f && alpha.y == 0.0f)) {
     const float nrm = sqrtf(alpha.x * alpha.x + alpha.y * alpha.y + xnorm2);
     beta = alpha.x >= 0.0f ? -nrm : nrm;
-    const float rb = 1.0f / beta;
+    const float rb = __frcp_rn(beta);  // == 1.0f / beta, without the division's slow path
     tau = make_float2((beta - alpha.x) * rb, -alpha.y * rb);
     // scale = 1 / (alpha - beta)
     const float2 am = make_float2(alpha.x - beta, alpha.y);
-    const float inv = 1.0f / (am.x * am.x + am.y * am.y);
+    const float inv = __frcp_rn(am.x * am.x + am.y * am.y);
     const float2 sc = make_float2(am.x * inv, -am.y * inv);
     for (int i = 1 + lane; i < m; i += 32) {
       const float2 v = cmul(A[(k + 1 + i) * ld + k], sc);
@@ -224,20 +224,33 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
       const int i = tid >> 1, h = tid & 1;
       float2 acc0 = make_float2(0.0f, 0.0f), acc1 = make_float2(0.0f, 0.0f);
       if (i < m) {
+        // row i below the diagonal, conj(column i) above it; four loads in
+        // flight before their products
+        const float2 *rowp = A22 + i * ld;
+        const float2 *colp = A22 + i;
         int j = h;
-        for (; j + 2 < m; j += 4) {
-          const float2 x0 = j <= i ? A22[i * ld + j] : make_float2(A22[j * ld + i].x, -A22[j * ld + i].y);
-          const int j1 = j + 2;
-          const float2 x1 = j1 <= i ? A22[i * ld + j1] : make_float2(A22[j1 * ld + i].x, -A22[j1 * ld + i].y);
-          const float2 t0 = cmul(x0, vb[j]);
-          const float2 t1 = cmul(x1, vb[j1]);
-          acc0.x += t0.x;
-          acc0.y += t0.y;
-          acc1.x += t1.x;
-          acc1.y += t1.y;
+        for (; j + 6 < m; j += 8) {
+          float2 x[4], vv[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int jj = j + 2 * u;
+            const float2 raw = jj <= i ? rowp[jj] : colp[jj * ld];
+            x[u] = jj <= i ? raw : make_float2(raw.x, -raw.y);
+            vv[u] = vb[jj];
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u += 2) {
+            const float2 t0 = cmul(x[u], vv[u]);
+            const float2 t1 = cmul(x[u + 1], vv[u + 1]);
+            acc0.x += t0.x;
+            acc0.y += t0.y;
+            acc1.x += t1.x;
+            acc1.y += t1.y;
+          }
         }
-        if (j < m) {
-          const float2 x0 = j <= i ? A22[i * ld + j] : make_float2(A22[j * ld + i].x, -A22[j * ld + i].y);
+        for (; j < m; j += 2) {
+          const float2 raw = j <= i ? rowp[j] : colp[j * ld];
+          const float2 x0 = j <= i ? raw : make_float2(raw.x, -raw.y);
           const float2 t0 = cmul(x0, vb[j]);
           acc0.x += t0.x;
           acc0.y += t0.y;
@@ -269,19 +282,65 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
       }
       const float cvv = 2.0f * (-0.5f * (tau.x * Dre - tau.y * Dim));
       if (warp == 0) {
-        // column 0 of A22 first, then reflector k+1 from it
+        // column 0 of A22 updated in registers (rows lane, lane + 32), and
+        // reflector k+1 formed from it at once (LAPACK zlarfg): alpha is row 1,
+        // x the rows below
         const float2 v0 = vb[0], p0 = pb[0];
-        for (int ii = lane; ii < m; ii += 32) {
-          const float2 vi = vb[ii], pi = pb[ii];
-          const float2 t1 = cmulc(vi, p0);
-          const float2 t2 = cmulc(pi, v0);
-          const float2 t3 = cmulc(vi, v0);
-          float2 *el = A22 + ii * ld;
-          const float2 old = *el;
-          *el = make_float2(old.x - t1.x - t2.x - cvv * t3.x, old.y - t1.y - t2.y - cvv * t3.y);
+        float2 col[2];
+        float part = 0.0f;
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+          const int ii = lane + 32 * t;
+          col[t] = make_float2(0.0f, 0.0f);
+          if (ii < m) {
+            const float2 vi = vb[ii], pi = pb[ii];
+            const float2 t1 = cmulc(vi, p0);
+            const float2 t2 = cmulc(pi, v0);
+            const float2 t3 = cmulc(vi, v0);
+            const float2 old = A22[ii * ld];
+            col[t] = make_float2(old.x - t1.x - t2.x - cvv * t3.x, old.y - t1.y - t2.y - cvv * t3.y);
+            if (ii >= 2) part += col[t].x * col[t].x + col[t].y * col[t].y;
+          }
         }
-        __syncwarp();
-        if (k + 1 < n - 1) make_reflector(A, ld, n, k + 1, vbuf, taus, e, lane);
+        const float2 alpha = make_float2(__shfl_sync(0xffffffffu, col[0].x, 1), __shfl_sync(0xffffffffu, col[0].y, 1));
+        const float xnorm2 = warp_sum(part);
+        if (lane < 2 && lane < m) A22[lane * ld] = col[0];  // diagonal element and alpha
+        if (k + 1 < n - 1) {
+          float2 tau1 = make_float2(0.0f, 0.0f);
+          float beta = alpha.x;
+          float2 sc = make_float2(1.0f, 0.0f);
+          const bool nonzero = !(xnorm2 == 0.0f && alpha.y == 0.0f);
+          if (nonzero) {
+            const float nrm = sqrtf(alpha.x * alpha.x + alpha.y * alpha.y + xnorm2);
+            beta = alpha.x >= 0.0f ? -nrm : nrm;
+            const float rb = __frcp_rn(beta);
+            tau1 = make_float2((beta - alpha.x) * rb, -alpha.y * rb);
+            const float2 am = make_float2(alpha.x - beta, alpha.y);  // scale = 1 / (alpha - beta)
+            const float inv = __frcp_rn(am.x * am.x + am.y * am.y);
+            sc = make_float2(am.x * inv, -am.y * inv);
+          }
+          float2 *vn = vbuf + ((k + 1) & 1) * n;
+#pragma unroll
+          for (int t = 0; t < 2; ++t) {
+            const int ii = lane + 32 * t;
+            if (ii >= 2 && ii < m) {
+              const float2 v = nonzero ? cmul(col[t], sc) : col[t];
+              A22[ii * ld] = v;
+              vn[ii - 1] = v;
+            }
+          }
+          if (lane == 0) {
+            vn[0] = make_float2(1.0f, 0.0f);
+            taus[k + 1] = tau1;
+            e[k + 1] = beta;
+          }
+        } else {
+#pragma unroll
+          for (int t = 0; t < 2; ++t) {
+            const int ii = lane + 32 * t;
+            if (ii >= 2 && ii < m) A22[ii * ld] = col[t];
+          }
+        }
       } else {
         // rows 1..m-1 of A22, columns 1..row: rows i and m-i (i and m-i
         // elements) share one pass of a warp
