@@ -484,7 +484,7 @@ int sf_run_corr_beam(sf_plan *plan, const int8_t *d_samples, const int16_t *d_sc
   int32_t *vis = d_vis ? d_vis : plan->d_vis;
   if (!d_samples || !d_scales || !d_beams_f16) return set_err(SF_ERR_INVALID_ARGUMENT, "NULL buffer");
   char why[160];
-  if (sf_correlate_supported(plan, why, sizeof(why)) && sf_beam_tc_supported(plan, plan->B) &&
+  if (sf_correlate_supported(plan, why, sizeof(why)) && sf_corrbeam_fused_supported(plan, plan->B) &&
       reinterpret_cast<uintptr_t>(d_samples) % 16 == 0) {
     // one pass over the samples: correlation and beams from the same tiles
     cudaStream_t s = as_stream(stream);
@@ -506,7 +506,7 @@ int sf_run_lambda_gpu(sf_plan *plan, const int8_t *d_samples, const int16_t *d_s
   float *evals = d_evals ? d_evals : plan->d_evals;
   if (!d_samples || !d_scales || !d_beams_f16) return set_err(SF_ERR_INVALID_ARGUMENT, "NULL buffer");
   char why[160];
-  if (sf_correlate_supported(plan, why, sizeof(why)) && sf_beam_tc_supported(plan, plan->B) &&
+  if (sf_correlate_supported(plan, why, sizeof(why)) && sf_corrbeam_fused_supported(plan, plan->B) &&
       reinterpret_cast<uintptr_t>(d_samples) % 16 == 0) {
     cudaStream_t s = as_stream(stream);
     SF_TRY(sf_launch_weights_plain(plan, s), "weights launch");

@@ -66,7 +66,7 @@ constexpr int WARP_CONV0 = 8;  // converters: warps 2-3 and 8-15
 constexpr int NUM_CONV_WARPS = 10;  // nine converting warps + one leader
 constexpr int NUM_CONV_THREADS = NUM_CONV_WARPS * 32;
 constexpr int NUM_WORKERS = NUM_CONV_WARPS - 1;  // warps that convert
-constexpr uint32_t BAR_START = 1, BAR_END = 2;  // named barriers of the converter group
+constexpr uint32_t BAR_START = 1;  // named barrier that opens a stage to the converter group
 constexpr int MAX_SLOTS = 32;
 constexpr int MAX_F = 64;
 constexpr uint32_t HEADER_BYTES = 3072;
@@ -93,8 +93,8 @@ struct CorrArgs {
   int slot_bytes;   // one packet of one channel: R * Tp * 4 bytes
   int slot_stride;  // slot_bytes + the packet's scales, rounded to 16
   int num_slots;    // packet ring depth (power of two)
-  uint32_t tp_magic;  // ceil(2^32 / Tp): q / Tp == umulhi(q, tp_magic) while q * Tp < 2^32
   int prefetch;     // ring deep enough to hold a stage's packets and the next stage's
+  uint32_t tp_magic;  // ceil(2^32 / Tp): q / Tp == umulhi(q, tp_magic) while q * Tp < 2^32
   int NB, NBW;      // beams written per pol; rows of weff per (c, p)
   int BN;           // beam MMA N = round_up(4 NB, 16)
   int katoms;       // 64-column K atoms of the weight tile: ceil(NR / 64)
@@ -122,6 +122,7 @@ struct __align__(8) Header {
   int rx_off[MAX_R];   // byte offset of receiver r's word at packet time 0 within a slot
   int rx_woff[MAX_R];  // window offset (samples) of receiver r's FPGA
   uint32_t unit_bits[2];  // per stage parity: bit s = ring slot s holds a packet whose scales are all 1
+  uint32_t stage_unit[2]; // per stage parity: every packet the stage reads has scales all 1
   int perm[2 * MAX_R];    // output stream 2 r + p <- source (src_r << 1) | src_pol, -1 = zero
   int n_items;
   int4 items[MAX_ITEMS];  // channel, first stage, end stage, whole (stored) or piece (atomics)
@@ -542,10 +543,15 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     // ---------------- converters ----------------
     // Nine warps convert; the leader warp acquires each stage's resources (the
     // stage's packets, with a flag per packet whose scales are all 1, and a
-    // free operand stage) one stage ahead, opens the stage to the converters
-    // with a named barrier, collects their completion on a second one
-    // (converters only arrive), and then signals the MMA issuer and returns
-    // the packets no later stage needs.
+    // free operand stage) one stage ahead and opens the stage to the
+    // converters with a named barrier.  Passing the barrier that opens stage
+    // pr also tells the leader that every converter has written stage pr - 1:
+    // only then does it signal the MMA issuer for pr - 1 and return the
+    // packets no later stage needs, so the converters themselves touch no
+    // mbarrier and these hand-offs overlap the conversion of stage pr.  After
+    // an item's last stage one more barrier closes it; so does one after
+    // every stage when the ring cannot hold two stages' packets (the next
+    // stage is then acquired once this one's packets are back).
     const int cwp = warp >= WARP_CONV0 ? warp - WARP_CONV0 + 2 : warp - 2;  // 0..9
     const int ct = cwp * 32 + lane;
     const bool leader = cwp == NUM_WORKERS;
@@ -577,25 +583,46 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     }
     // leader state
     uint32_t unit_bits = 0;  // bit s = ring slot s holds a packet whose scales are all 1
-    int q_rel = 0, q_wait = 0;
+    int q_rel = 0;           // first packet not yet returned to the producer
+    int q_wait = 0;          // first packet not yet waited for
     bool acq_ok = true;
     // leader: wait for the packets of stage pr of the current channel and a
     // free operand stage for op_iter_next; publish the packet flags
     auto acquire = [&](int pr, uint32_t gq0, uint32_t it) {
       const int s0 = pr * TILE_T;
-      const int qb = s0 < T ? min(a.P + 1, (min(s0 + TILE_T - 1, T - 1) + off_max) / Tp) : q_hi(npairs);
+      const int qb = s0 < T ? min(a.P + 1, static_cast<int>(__umulhi(static_cast<uint32_t>(min(s0 + TILE_T - 1, T - 1) + off_max), a.tp_magic)))
+                            : q_hi(npairs);
       bool ok = true;
+      const int q0 = q_wait;
       for (; q_wait <= qb && ok; ++q_wait) {
         const uint32_t gq = gq0 + q_wait;
-        const uint32_t sl = gq & ns_mask;
-        ok = mbar_wait(&h.pk_full[sl], (gq >> ns_shift) & 1u, abort_flag, SUSPEND_NS);
-        bool unit = true;
-        for (int r = lane; r < R; r += 32) unit &= lds32(ring_s + sl * sstride + a.slot_bytes + r * 4) == 0x00010001u;
-        unit = __all_sync(0xffffffffu, unit);
-        unit_bits = unit ? (unit_bits | (1u << sl)) : (unit_bits & ~(1u << sl));
+        ok = mbar_wait(&h.pk_full[gq & ns_mask], (gq >> ns_shift) & 1u, abort_flag, SUSPEND_NS);
       }
+      // scale flags of the new packets, two at a time: lanes 16 h + j read
+      // scale words 4 j .. 4 j + 3 (R <= 48) of packet q + h
+      for (int q = q0; q < q_wait; q += 2) {
+        const int h2 = lane >> 4, j = lane & 15;
+        const uint32_t sl = (gq0 + q + h2) & ns_mask;
+        bool unit = true;
+        if (q + h2 < q_wait && 4 * j < R) {
+          const uint4 v = lds128(ring_s + sl * sstride + a.slot_bytes + 16 * j);
+          unit = (v.x == 0x00010001u) && (4 * j + 1 >= R || v.y == 0x00010001u) &&
+                 (4 * j + 2 >= R || v.z == 0x00010001u) && (4 * j + 3 >= R || v.w == 0x00010001u);
+        }
+        const uint32_t bad = __ballot_sync(0xffffffffu, !unit);
+        const uint32_t sl0 = (gq0 + q) & ns_mask, sl1 = (gq0 + q + 1) & ns_mask;
+        unit_bits = (bad & 0xffffu) ? (unit_bits & ~(1u << sl0)) : (unit_bits | (1u << sl0));
+        if (q + 1 < q_wait) unit_bits = (bad >> 16) ? (unit_bits & ~(1u << sl1)) : (unit_bits | (1u << sl1));
+      }
+      // the whole stage on unit scales?
+      uint32_t su = 1u;
+      for (int q = static_cast<int>(__umulhi(static_cast<uint32_t>(s0 + off_min), a.tp_magic)); q <= qb; ++q)
+        su &= unit_bits >> ((gq0 + q) & ns_mask);
       ok = ok && mbar_wait(&h.op_empty[it & 1u], ((it >> 1) & 1u) ^ 1u, abort_flag, SUSPEND_NS);
-      if (lane == 0) h.unit_bits[it & 1u] = unit_bits;
+      if (lane == 0) {
+        h.unit_bits[it & 1u] = unit_bits;
+        h.stage_unit[it & 1u] = su & 1u;
+      }
       if (!ok) {
         failed = true;
         if (lane == 0) *abort_flag = 1;
@@ -653,27 +680,32 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
         q_wait = qlo;
         acq_ok = acquire(pb, gq0, op_iter);
       }
+      // first packet a stage starting at sample s reads
+      auto first_packet = [&](int s) { return static_cast<int>(__umulhi(static_cast<uint32_t>(s + off_min), a.tp_magic)); };
+      // leader: stage `st` is written; return packets below `next`
+      auto hand_off = [&](uint32_t st, int next) {
+        if (lane == 0) {
+          mbar_arrive(&h.op_full[st]);
+          for (; q_rel < next; ++q_rel) mbar_arrive(&h.pk_empty[(gq0 + q_rel) & ns_mask]);
+        }
+        __syncwarp();
+      };
       for (int pr = pb; pr < pe; ++pr) {
         const int s0 = pr * TILE_T;
         const uint32_t st = op_iter & 1u;
         named_bar_sync(BAR_START, NUM_CONV_THREADS);  // stage pr is open
         if (leader) {
+          // stage pr - 1 is written: to the MMA issuer, with its packets
+          // below stage pr's first
+          if (pr > pb && a.prefetch) hand_off(st ^ 1u, first_packet(s0));
           // the next stage's resources while the converters work
-          const bool more = pr + 1 < pe;
-          if (more && a.prefetch) acq_ok = acquire(pr + 1, gq0, op_iter + 1);
-          named_bar_sync(BAR_END, NUM_CONV_THREADS);  // every converter is done with stage pr
-          if (lane == 0) {
-            mbar_arrive(&h.op_full[st]);
-            // packets no later stage needs go back to the producer
-            int next = qhi + 1;
-            if (more && s0 + TILE_T < T) next = (s0 + TILE_T + off_min) / Tp;
-            for (; q_rel < next; ++q_rel) mbar_arrive(&h.pk_empty[(gq0 + q_rel) & ns_mask]);
-          }
-          __syncwarp();
-          if (more && !a.prefetch) acq_ok = acquire(pr + 1, gq0, op_iter + 1);
+          if (pr + 1 < pe && a.prefetch) acq_ok = acquire(pr + 1, gq0, op_iter + 1);
         } else {
           const bool ok = *abort_flag == 0;
           const uint32_t ubits = *reinterpret_cast<volatile uint32_t *>(&h.unit_bits[st]);
+          // every packet of the stage on unit scales and every sample inside the
+          // integration: no per-sample scale or range tests
+          const bool stage_fast = *reinterpret_cast<volatile uint32_t *>(&h.stage_unit[st]) != 0u && s0 + TILE_T <= T;
           const uint32_t stage_s = op_s + st * stage_bytes;
           if (ok && a.perm) {
             // permuted streams (reorder_streams semantics): every output stream
@@ -704,6 +736,43 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
                     xi = static_cast<float>(static_cast<int8_t>(raw >> 8) * sc);
                   }
                   o[e] = u32_of(__floats2half2_rn(xr, xi));  // fp16(x * scale)
+                }
+                sts128(stage_s + stoff[k] + g * (32 * 128), o[0], o[1], o[2], o[3]);
+              }
+            }
+          } else if (ok && stage_fast) {
+#pragma unroll
+            for (int k = 0; k < MAX_JP; ++k) {
+              const int jp = cwp + NUM_WORKERS * k;
+              if (jp >= nrp) break;
+              uint32_t wd[4][2];
+#pragma unroll
+              for (int g = 0; g < 4; ++g) {
+                const int t = s0 + g * 32 + lane;
+                uint32_t qq = static_cast<uint32_t>(t + woff0[k]);
+                uint32_t pkt = __umulhi(qq, a.tp_magic);
+                uint32_t tt = qq - pkt * static_cast<uint32_t>(Tp);
+                const uint32_t a0 = ring_s + ((gq0 + pkt) & ns_mask) * sstride + roff0[k] + tt * Rpp4;
+                uint32_t a1 = a0 + dr1[k];
+                if (!same[k]) {
+                  qq = static_cast<uint32_t>(t + woff1[k]);
+                  pkt = __umulhi(qq, a.tp_magic);
+                  tt = qq - pkt * static_cast<uint32_t>(Tp);
+                  a1 = ring_s + ((gq0 + pkt) & ns_mask) * sstride + roff0[k] + dr1[k] + tt * Rpp4;
+                }
+                wd[g][0] = lds32(a0);
+                wd[g][1] = has1[k] ? lds32(a1) : 0u;
+              }
+#pragma unroll
+              for (int g = 0; g < 4; ++g) {
+                // x -> fp16(x) by the 1024 + b bias trick
+                uint32_t o[4];
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                  const uint32_t biased = wd[g][e] ^ 0x80808080u;
+                  const __half2 bias = h2_of(0x64806480u);  // 1152
+                  o[2 * e] = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4140)), bias));
+                  o[2 * e + 1] = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4342)), bias));
                 }
                 sts128(stage_s + stoff[k] + g * (32 * 128), o[0], o[1], o[2], o[3]);
               }
@@ -769,10 +838,19 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
             }
           }
           fence_proxy_async_smem();
-          named_bar_arrive(BAR_END, NUM_CONV_THREADS);  // done with stage pr
         }
         ++op_iter;
+        if (!a.prefetch && pr + 1 < pe) {
+          named_bar_sync(BAR_START, NUM_CONV_THREADS);  // stage pr is written
+          if (leader) {
+            hand_off(st, first_packet(s0 + TILE_T));
+            acq_ok = acquire(pr + 1, gq0, op_iter);
+          }
+        }
       }
+      // the item's last stage is written: to the MMA issuer, with every packet
+      named_bar_sync(BAR_START, NUM_CONV_THREADS);
+      if (leader) hand_off((op_iter - 1) & 1u, qhi + 1);
       g_base += qhi - qlo + 1;
     }
     (void)acq_ok;
@@ -832,6 +910,17 @@ int sf_correlate_supported(const sf_plan *p, char *why, size_t why_len) {
 
 int sf_beam_tc_supported(const sf_plan *p, int n_beams_out) {
   return sf_correlate_supported(p, nullptr, 0) && n_beams_out <= MAX_BEAM_OUT;
+}
+
+// One pass producing both visibilities and beams: the fp32 chunk accumulator,
+// the int32 running sums and two beam tiles share the 512 tensor-memory
+// columns.
+int sf_corrbeam_fused_supported(const sf_plan *p, int n_beams_out) {
+  if (!sf_beam_tc_supported(p, n_beams_out)) return 0;
+  const int NR = ((4 * p->R + 15) / 16) * 16;
+  const int ncols = NR + (NR > 128 ? NR - 128 : 0);
+  const int BN = ((4 * n_beams_out + 15) / 16) * 16;
+  return 2 * ncols + 2 * BN <= 512;
 }
 
 // mode bit 0: correlate, bit 1: beamform (n_beams_out beams per pol from the

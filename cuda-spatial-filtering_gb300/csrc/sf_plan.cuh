@@ -66,6 +66,7 @@ cudaError_t sf_launch_corrbeam(const sf_plan *p, const int8_t *samples, const in
                                const int32_t *offsets, int32_t *vis, int n_beams_out, __half2 *beams,
                                int mode, cudaStream_t stream);
 int sf_beam_tc_supported(const sf_plan *p, int n_beams_out);
+int sf_corrbeam_fused_supported(const sf_plan *p, int n_beams_out);
 
 cudaError_t sf_launch_eig(const sf_plan *p, const int32_t *vis, int eig_mode, int k_rule,
                           float delta, int shrink, float *evals, float2 *evecs, int32_t *counts,

@@ -102,6 +102,9 @@ def _correlate_gpu(sh, samples, scales, window, delays=None):
     (32, 4, 32, 5, sfgb.SF_WINDOW_ALIGNED, [1, 2, 3, -32]),
     (40, 4, 64, 3, sfgb.SF_WINDOW_ALIGNED, [0, 0, 1, 1]),
     (48, 6, 16, 9, sfgb.SF_WINDOW_ALIGNED, [0, -16, 16, 5, -5, 9]),
+    # 9.4 KB packets: the ring holds one stage's packets but not two, so each
+    # stage is closed before the next one's packets are acquired
+    (48, 4, 48, 9, sfgb.SF_WINDOW_ALIGNED, [0, 12, -48, 48]),
 ])
 def test_correlator_bit_exact_random(R, F, Tp, P, window, delays):
     sh = orc.Shape(3, F, Tp, R, R // F, P, 1)
@@ -537,6 +540,28 @@ def test_adaptive_chain_split_channels(split_case):
 
 def test_corr_beam_fused_split_channels(split_case):
     sh, samples, scales, weights = split_case
+    plan = sfgb.Plan(sh.C, sh.F, sh.Tp, sh.R, sh.Rpp, sh.P, sh.B)
+    plan.set_weights(weights)
+    s, sc = _dev(samples, torch.int8), _dev(scales, torch.int16)
+    vis = torch.full(plan.vis_shape(), -7, dtype=torch.int32, device="cuda")
+    beams = torch.empty(plan.beams_shape(1), dtype=torch.float16, device="cuda")
+    plan.run_corr_beam(s, sc, vis, beams)
+    torch.cuda.synchronize()
+    rc, bits = plan.status()
+    assert rc == 0 and bits == 0
+    plan.close()
+    ref = orc.corr_beam_chain(sh, samples, scales, weights)
+    assert np.array_equal(vis.cpu().numpy(), ref["vis"])
+    _beam_close(beams.cpu().numpy().astype(np.float32), ref["beams"], sh.B)
+
+
+def test_shallow_packet_ring_corr_beam_split_channels():
+    """Tp = 48, R = 48: an eight-slot packet ring, too shallow to hold two
+    stages' packets at once, so the converters close every stage before the
+    next one is acquired; 200 channels also split into single-stage pieces."""
+    sh = orc.Shape(200, 4, 48, 48, 12, 9, 4)
+    samples, scales, _ = orc.synth_inputs(sh, seed=41, n_interferers=2, frac_channels=0.5)
+    weights = orc.synth_weights(sh, seed=42)
     plan = sfgb.Plan(sh.C, sh.F, sh.Tp, sh.R, sh.Rpp, sh.P, sh.B)
     plan.set_weights(weights)
     s, sc = _dev(samples, torch.int8), _dev(scales, torch.int16)
