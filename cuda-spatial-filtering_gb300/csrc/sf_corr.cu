@@ -740,6 +740,43 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
                 sts128(stage_s + stoff[k] + g * (32 * 128), o[0], o[1], o[2], o[3]);
               }
             }
+          } else if (ok && stage_fast && off_min == off_max) {
+            // one window offset for every FPGA: a lane's packet slot and time
+            // within the packet are the same for every receiver, so each
+            // 32-sample group's address is formed once
+            uint32_t base[4];
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+              const uint32_t qq = static_cast<uint32_t>(s0 + g * 32 + lane + off_min);
+              const uint32_t pkt = __umulhi(qq, a.tp_magic);
+              const uint32_t tt = qq - pkt * static_cast<uint32_t>(Tp);
+              base[g] = ring_s + ((gq0 + pkt) & ns_mask) * sstride + tt * Rpp4;
+            }
+#pragma unroll
+            for (int k = 0; k < MAX_JP; ++k) {
+              const int jp = cwp + NUM_WORKERS * k;
+              if (jp >= nrp) break;
+              uint32_t wd[4][2];
+#pragma unroll
+              for (int g = 0; g < 4; ++g) {
+                const uint32_t a0 = base[g] + roff0[k];
+                wd[g][0] = lds32(a0);
+                wd[g][1] = has1[k] ? lds32(a0 + dr1[k]) : 0u;
+              }
+#pragma unroll
+              for (int g = 0; g < 4; ++g) {
+                // x -> fp16(x) by the 1024 + b bias trick
+                uint32_t o[4];
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                  const uint32_t biased = wd[g][e] ^ 0x80808080u;
+                  const __half2 bias = h2_of(0x64806480u);  // 1152
+                  o[2 * e] = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4140)), bias));
+                  o[2 * e + 1] = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4342)), bias));
+                }
+                sts128(stage_s + stoff[k] + g * (32 * 128), o[0], o[1], o[2], o[3]);
+              }
+            }
           } else if (ok && stage_fast) {
 #pragma unroll
             for (int k = 0; k < MAX_JP; ++k) {
