@@ -545,10 +545,9 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
             x2 = x1;
             x1 = v;
           }
-          float s2 = 0.0f;
-          for (int i = 0; i < n; ++i) s2 += x[i] * x[i];
-          const float inv = s2 > 0.0f ? rsqrtf(s2) : 0.0f;
-          for (int i = 0; i < n; ++i) x[i] *= inv;
+          // no normalisation here: the Gram-Schmidt pass below normalises
+          // (one solve grows a unit vector by at most about 1 / pert, far
+          // inside the float range)
         }
         __syncwarp();
         // modified Gram-Schmidt of this group's vectors against all earlier ones
