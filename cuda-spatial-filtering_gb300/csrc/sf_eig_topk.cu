@@ -102,6 +102,8 @@ __device__ __forceinline__ int sturm_count(const float *d, const float *e2, int 
   float q = d[0] - x;
   if (fabsf(q) < pivmin) q = -pivmin;
   cnt += q < 0.0f;
+  // unrolled so that the loads of d and e2 run ahead of the recurrence
+#pragma unroll 4
   for (int i = 1; i < n; ++i) {
     q = d[i] - x - __fdividef(e2[i - 1], q);
     if (fabsf(q) < pivmin) q = -pivmin;
@@ -404,16 +406,32 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
   // stable solver reaches (and what detection and the shifts need)
   const float atol = 2.4e-7f * tnorm + 4.0f * pivmin;
   if (need_all) {
-    // every eigenvalue, one thread each, by bisection
-    for (int j = tid; j < n; j += NT) {
+    // every eigenvalue by 4-way multisection, three lanes each (lanes 3 s ..
+    // 3 s + 2 of a warp, s < 10), each lane counting at one interior point:
+    // two bits of the bracket per Sturm count instead of bisection's one
+    const int slot = lane / 3, sub = lane - 3 * slot;
+    for (int j0 = 0; j0 < n; j0 += 10 * NW) {
+      const int j = j0 + warp * 10 + slot;
+      const bool mine = slot < 10 && j < n;
       float lo = glo, hi = ghi;
+      bool done = !mine;
       for (int it = 0; it < 64; ++it) {
-        const float mid = 0.5f * (lo + hi);
-        if (hi - lo <= atol || mid == lo || mid == hi) break;
-        if (sturm_count(d, e2, n, mid, pivmin) > j) hi = mid;
-        else lo = mid;
+        if (__all_sync(0xffffffffu, done)) break;
+        const float step = (hi - lo) * 0.25f;
+        const float x = lo + step * static_cast<float>(sub + 1);
+        const bool above = !done && sturm_count(d, e2, n, x, pivmin) > j;
+        // eigenvalue j lies in [x_{f-1}, x_f), f = first point with more than j below it
+        const unsigned grp = (__ballot_sync(0xffffffffu, above) >> (3 * min(slot, 9))) & 7u;
+        if (!done) {
+          const int f = grp ? __ffs(grp) - 1 : 3;
+          const float nlo = f == 0 ? lo : lo + step * static_cast<float>(f);
+          const float nhi = f == 3 ? hi : lo + step * static_cast<float>(f + 1);
+          done = !(step > 0.0f) || (nlo == lo && nhi == hi) || nhi - nlo <= atol;
+          lo = nlo;
+          hi = nhi;
+        }
       }
-      lam[j] = 0.5f * (lo + hi);
+      if (mine && sub == 0) lam[j] = 0.5f * (lo + hi);
     }
   } else {
     // the top K only, one warp each: 33-way multisection (32 interior points)
@@ -476,6 +494,7 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
         const int r = g0 + lane;
         const float shift = lam[n - 1 - r];
         float cd = d[0] - shift, cs = n > 1 ? e[0] : 0.0f;
+#pragma unroll 4
         for (int i = 0; i < n - 1; ++i) {
           const float sub = e[i];
           const float nd = d[i + 1] - shift;
@@ -518,6 +537,7 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
           // forward: the row interchanges and multipliers of the factorisation
           // (the running value stays in a register)
           float cur = x[0];
+#pragma unroll 4
           for (int i = 0; i < n - 1; ++i) {
             float nxt = x[i + 1];
             if (pv[i] != 0.0f) {
@@ -539,6 +559,7 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
             x2 = x1;
             x1 = v;
           }
+#pragma unroll 4
           for (int i = n - 3; i >= 0; --i) {
             const float v = (x[i] - u1[i] * x1 - u2[i] * x2) * u0[i];
             x[i] = v;
