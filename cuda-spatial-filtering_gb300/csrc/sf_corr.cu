@@ -66,6 +66,7 @@ constexpr int WARP_CONV0 = 8;  // converters: warps 2-3 and 8-15
 constexpr int NUM_CONV_WARPS = 10;  // nine converting warps + one leader
 constexpr int NUM_CONV_THREADS = NUM_CONV_WARPS * 32;
 constexpr int NUM_WORKERS = NUM_CONV_WARPS - 1;  // warps that convert
+constexpr int HANDOFF_CWP = 3;  // converting warp that also hands finished stages on
 constexpr uint32_t BAR_START = 1;  // named barrier that opens a stage to the converter group
 constexpr int MAX_SLOTS = 32;
 constexpr int MAX_F = 64;
@@ -545,16 +546,18 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     // stage's packets, with a flag per packet whose scales are all 1, and a
     // free operand stage) one stage ahead and opens the stage to the
     // converters with a named barrier.  Passing the barrier that opens stage
-    // pr also tells the leader that every converter has written stage pr - 1:
-    // only then does it signal the MMA issuer for pr - 1 and return the
-    // packets no later stage needs, so the converters themselves touch no
-    // mbarrier and these hand-offs overlap the conversion of stage pr.  After
-    // an item's last stage one more barrier closes it; so does one after
-    // every stage when the ring cannot hold two stages' packets (the next
-    // stage is then acquired once this one's packets are back).
+    // pr also tells every warp that stage pr - 1 is written: one converting
+    // warp (HANDOFF_CWP) then signals the MMA issuer for pr - 1 and returns
+    // the packets no later stage needs before it converts its share of pr,
+    // so the leader only acquires and the other converters touch no
+    // mbarrier.  After an item's last stage one more barrier closes it; so
+    // does one after every stage when the ring cannot hold two stages'
+    // packets (the next stage is then acquired once this one's packets are
+    // back).
     const int cwp = warp >= WARP_CONV0 ? warp - WARP_CONV0 + 2 : warp - 2;  // 0..9
     const int ct = cwp * 32 + lane;
     const bool leader = cwp == NUM_WORKERS;
+    const bool handoff = cwp == HANDOFF_CWP;
     uint32_t g_base = 0, op_iter = 0, cw = 0;
     bool failed = false;
     const int nrp = (R + 1) >> 1;  // receiver pairs = 16-byte chunks per sample
@@ -581,10 +584,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
       has1[k] = 2 * jp + 1 < R;
       stoff[k] = (jp >> 3) * ATOM_BYTES + lane * 128 + (((jp & 7) ^ (lane & 7)) << 4);
     }
-    // leader state
-    uint32_t unit_bits = 0;  // bit s = ring slot s holds a packet whose scales are all 1
-    int q_rel = 0;           // first packet not yet returned to the producer
-    int q_wait = 0;          // first packet not yet waited for
+    uint32_t unit_bits = 0;  // leader: bit s = ring slot s holds a packet whose scales are all 1
+    int q_rel = 0;           // hand-off warp: first packet not yet returned to the producer
+    int q_wait = 0;          // leader: first packet not yet waited for
     bool acq_ok = true;
     // leader: wait for the packets of stage pr of the current channel and a
     // free operand stage for op_iter_next; publish the packet flags
@@ -675,14 +677,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
         if (lane == 0) mbar_arrive(&h.w_full[wb]);
       }
       const uint32_t gq0 = g_base - static_cast<uint32_t>(qlo);  // ring index of packet q: gq0 + q
+      q_rel = qlo;
       if (leader) {
-        q_rel = qlo;
         q_wait = qlo;
         acq_ok = acquire(pb, gq0, op_iter);
       }
       // first packet a stage starting at sample s reads
       auto first_packet = [&](int s) { return static_cast<int>(__umulhi(static_cast<uint32_t>(s + off_min), a.tp_magic)); };
-      // leader: stage `st` is written; return packets below `next`
+      // hand-off warp: stage `st` is written; return packets below `next`
       auto hand_off = [&](uint32_t st, int next) {
         if (lane == 0) {
           mbar_arrive(&h.op_full[st]);
@@ -695,12 +697,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
         const uint32_t st = op_iter & 1u;
         named_bar_sync(BAR_START, NUM_CONV_THREADS);  // stage pr is open
         if (leader) {
-          // stage pr - 1 is written: to the MMA issuer, with its packets
-          // below stage pr's first
-          if (pr > pb && a.prefetch) hand_off(st ^ 1u, first_packet(s0));
           // the next stage's resources while the converters work
           if (pr + 1 < pe && a.prefetch) acq_ok = acquire(pr + 1, gq0, op_iter + 1);
         } else {
+          // stage pr - 1 is written: to the MMA issuer, with its packets
+          // below stage pr's first
+          if (handoff && pr > pb && a.prefetch) hand_off(st ^ 1u, first_packet(s0));
           const bool ok = *abort_flag == 0;
           const uint32_t ubits = *reinterpret_cast<volatile uint32_t *>(&h.unit_bits[st]);
           // every packet of the stage on unit scales and every sample inside the
@@ -879,15 +881,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
         ++op_iter;
         if (!a.prefetch && pr + 1 < pe) {
           named_bar_sync(BAR_START, NUM_CONV_THREADS);  // stage pr is written
-          if (leader) {
-            hand_off(st, first_packet(s0 + TILE_T));
-            acq_ok = acquire(pr + 1, gq0, op_iter);
-          }
+          if (handoff) hand_off(st, first_packet(s0 + TILE_T));
+          if (leader) acq_ok = acquire(pr + 1, gq0, op_iter);
         }
       }
       // the item's last stage is written: to the MMA issuer, with every packet
       named_bar_sync(BAR_START, NUM_CONV_THREADS);
-      if (leader) hand_off((op_iter - 1) & 1u, qhi + 1);
+      if (handoff) hand_off((op_iter - 1) & 1u, qhi + 1);
       g_base += qhi - qlo + 1;
     }
     (void)acq_ok;
