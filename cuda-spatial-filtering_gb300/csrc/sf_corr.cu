@@ -56,7 +56,7 @@ constexpr int KBLK = 64;         // samples per K block (chunk accounting)
 constexpr int TILE_T = 128;      // samples per operand stage
 constexpr uint32_t ATOM_BYTES = TILE_T * 128;  // one 64-value atom of a stage
 constexpr int CHUNK_KBLK = 16;   // K blocks per exact fp32 chunk (1024 samples)
-constexpr int NUM_OP_STAGES = 2;
+constexpr int MAX_OP_STAGES = 3;  // operand stages (two or three, as shared memory allows)
 constexpr int NUM_WARPS = 16;
 constexpr int NTHREADS = NUM_WARPS * 32;
 constexpr int WARP_TMA = 0;
@@ -94,6 +94,7 @@ struct CorrArgs {
   int slot_bytes;   // one packet of one channel: R * Tp * 4 bytes
   int slot_stride;  // slot_bytes + the packet's scales, rounded to 16
   int num_slots;    // packet ring depth (power of two)
+  int nstages;      // operand stages: 3 when they fit beside a ring deep enough to prefetch, else 2
   int prefetch;     // ring deep enough to hold a stage's packets and the next stage's
   uint32_t tp_magic;  // ceil(2^32 / Tp): q / Tp == umulhi(q, tp_magic) while q * Tp < 2^32
   int NB, NBW;      // beams written per pol; rows of weff per (c, p)
@@ -108,8 +109,8 @@ struct CorrArgs {
 struct __align__(8) Header {
   uint64_t pk_full[MAX_SLOTS];
   uint64_t pk_empty[MAX_SLOTS];
-  uint64_t op_full[NUM_OP_STAGES];
-  uint64_t op_empty[NUM_OP_STAGES];
+  uint64_t op_full[MAX_OP_STAGES];
+  uint64_t op_empty[MAX_OP_STAGES];
   uint64_t acc_full[2];
   uint64_t acc_empty[2];
   uint64_t beam_full[2];
@@ -122,8 +123,8 @@ struct __align__(8) Header {
   int offsets[MAX_F];
   int rx_off[MAX_R];   // byte offset of receiver r's word at packet time 0 within a slot
   int rx_woff[MAX_R];  // window offset (samples) of receiver r's FPGA
-  uint32_t unit_bits[2];  // per stage parity: bit s = ring slot s holds a packet whose scales are all 1
-  uint32_t stage_unit[2]; // per stage parity: every packet the stage reads has scales all 1
+  uint32_t unit_bits[MAX_OP_STAGES];   // per operand stage: bit s = ring slot s holds a packet whose scales are all 1
+  uint32_t stage_unit[MAX_OP_STAGES];  // per operand stage: every packet the stage reads has scales all 1
   int perm[2 * MAX_R];    // output stream 2 r + p <- source (src_r << 1) | src_pol, -1 = zero
   int n_items;
   int4 items[MAX_ITEMS];  // channel, first stage, end stage, whole (stored) or piece (atomics)
@@ -238,8 +239,15 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
   const uint32_t op_addr = (sbase + HEADER_BYTES + 1023u) & ~1023u;
   uint8_t *op_ptr = smem + (op_addr - sbase);
   const uint32_t stage_bytes = static_cast<uint32_t>(a.natoms) * ATOM_BYTES;
-  const uint32_t w_addr = op_addr + NUM_OP_STAGES * stage_bytes;  // weight tiles (1024-aligned)
-  uint8_t *w_ptr = op_ptr + NUM_OP_STAGES * stage_bytes;
+  const uint32_t SO = static_cast<uint32_t>(a.nstages);
+  const uint32_t w_addr = op_addr + SO * stage_bytes;  // weight tiles (1024-aligned)
+  uint8_t *w_ptr = op_ptr + SO * stage_bytes;
+  // operand stage of the it-th stage processed and the parity of its use
+  auto stage_of = [&](uint32_t it, uint32_t &st, uint32_t &ph) {
+    const uint32_t q = SO == 2u ? it >> 1 : __umulhi(it, 0x55555556u);  // it / SO
+    st = it - q * SO;
+    ph = q & 1u;
+  };
   uint8_t *ring_ptr = w_ptr + (DO_BEAM ? 2 * a.wtile_bytes : 0u);
   const int NS = a.num_slots;
   const uint32_t ns_mask = static_cast<uint32_t>(NS - 1);
@@ -250,7 +258,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
       mbar_init(&h.pk_full[s], 1 + 32);
       mbar_init(&h.pk_empty[s], 1);
     }
-    for (int s = 0; s < NUM_OP_STAGES; ++s) {
+    for (int s = 0; s < a.nstages; ++s) {
       mbar_init(&h.op_full[s], 1);
       mbar_init(&h.op_empty[s], 1);
     }
@@ -286,7 +294,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
   // read as zero; the converters never write them.
   {
     uint4 *z = reinterpret_cast<uint4 *>(op_ptr);
-    const int n16 = (NUM_OP_STAGES * stage_bytes + (DO_BEAM ? 2 * a.wtile_bytes : 0u)) / 16;
+    const int n16 = (SO * stage_bytes + (DO_BEAM ? 2 * a.wtile_bytes : 0u)) / 16;
     for (int i = tid; i < n16; i += NTHREADS) z[i] = make_uint4(0, 0, 0, 0);
     fence_proxy_async_smem();
   }
@@ -371,8 +379,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
         if (DO_BEAM) failed |= !mbar_wait(&h.w_full[wb], (cw >> 1) & 1u, abort_flag, SUSPEND_NS);
         const uint32_t woff = wb * a.wtile_bytes;
         for (int pr = pb; pr < pe; ++pr) {
-          const uint32_t st = op_iter & 1u;
-          bool ok = mbar_wait(&h.op_full[st], (op_iter >> 1) & 1u, abort_flag, SUSPEND_NS);
+          uint32_t st, ph;
+          stage_of(op_iter, st, ph);
+          bool ok = mbar_wait(&h.op_full[st], ph, abort_flag, SUSPEND_NS);
           tc_fence_after();
           const uint32_t soff = st * stage_bytes;
           if (DO_CORR) {
@@ -620,10 +629,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
       uint32_t su = 1u;
       for (int q = static_cast<int>(__umulhi(static_cast<uint32_t>(s0 + off_min), a.tp_magic)); q <= qb; ++q)
         su &= unit_bits >> ((gq0 + q) & ns_mask);
-      ok = ok && mbar_wait(&h.op_empty[it & 1u], ((it >> 1) & 1u) ^ 1u, abort_flag, SUSPEND_NS);
+      uint32_t ist, iph;
+      stage_of(it, ist, iph);
+      ok = ok && mbar_wait(&h.op_empty[ist], iph ^ 1u, abort_flag, SUSPEND_NS);
       if (lane == 0) {
-        h.unit_bits[it & 1u] = unit_bits;
-        h.stage_unit[it & 1u] = su & 1u;
+        h.unit_bits[ist] = unit_bits;
+        h.stage_unit[ist] = su & 1u;
       }
       if (!ok) {
         failed = true;
@@ -694,7 +705,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
       };
       for (int pr = pb; pr < pe; ++pr) {
         const int s0 = pr * TILE_T;
-        const uint32_t st = op_iter & 1u;
+        uint32_t st, ph;
+        stage_of(op_iter, st, ph);
         named_bar_sync(BAR_START, NUM_CONV_THREADS);  // stage pr is open
         if (leader) {
           // the next stage's resources while the converters work
@@ -702,7 +714,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
         } else {
           // stage pr - 1 is written: to the MMA issuer, with its packets
           // below stage pr's first
-          if (handoff && pr > pb && a.prefetch) hand_off(st ^ 1u, first_packet(s0));
+          if (handoff && pr > pb && a.prefetch) hand_off(st == 0u ? SO - 1u : st - 1u, first_packet(s0));
           const bool ok = *abort_flag == 0;
           const uint32_t ubits = *reinterpret_cast<volatile uint32_t *>(&h.unit_bits[st]);
           // every packet of the stage on unit scales and every sample inside the
@@ -887,7 +899,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
       }
       // the item's last stage is written: to the MMA issuer, with every packet
       named_bar_sync(BAR_START, NUM_CONV_THREADS);
-      if (handoff) hand_off((op_iter - 1) & 1u, qhi + 1);
+      if (handoff) {
+        uint32_t lst, lph;
+        stage_of(op_iter - 1u, lst, lph);
+        hand_off(lst, qhi + 1);
+      }
       g_base += qhi - qlo + 1;
     }
     (void)acq_ok;
@@ -1022,16 +1038,25 @@ cudaError_t sf_launch_corrbeam(const sf_plan *p, const int8_t *samples, const in
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&g_max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   }
-  const size_t fixed = HEADER_BYTES + 1024 + (size_t)NUM_OP_STAGES * a.natoms * ATOM_BYTES + 2 * a.wtile_bytes;
   // packets one stage touches: (TILE_T - 1 + window spread <= 2 Tp) / Tp + 2, plus one in flight
   const int need_slots = (TILE_T - 1) / p->Tp + 5;
-  long avail = (long)g_max_smem - (long)fixed;
-  int ns = avail > 0 ? (int)std::min<long>(MAX_SLOTS, avail / a.slot_stride) : 0;
-  while (ns & (ns - 1)) ns &= ns - 1;  // round down to a power of two
+  const int prefetch_slots = (2 * TILE_T - 1) / p->Tp + 5;
+  // ring depth beside `stages` operand stages (a power of two)
+  auto ring_depth = [&](int stages) {
+    const long fixed = HEADER_BYTES + 1024 + (long)stages * a.natoms * ATOM_BYTES + 2 * (long)a.wtile_bytes;
+    const long avail = (long)g_max_smem - fixed;
+    int ns = avail > 0 ? (int)std::min<long>(MAX_SLOTS, avail / a.slot_stride) : 0;
+    while (ns & (ns - 1)) ns &= ns - 1;  // round down to a power of two
+    return ns;
+  };
+  // a third operand stage lets the converters run a stage ahead of the MMAs
+  a.nstages = ring_depth(3) >= prefetch_slots ? 3 : 2;
+  const int ns = ring_depth(a.nstages);
   if (ns < need_slots) return cudaErrorInvalidConfiguration;
   a.num_slots = ns;
-  a.prefetch = ns >= (2 * TILE_T - 1) / p->Tp + 5 ? 1 : 0;
-  const size_t smem = fixed + (size_t)ns * a.slot_stride;
+  a.prefetch = ns >= prefetch_slots ? 1 : 0;
+  const size_t smem = HEADER_BYTES + 1024 + (size_t)a.nstages * a.natoms * ATOM_BYTES + 2 * (size_t)a.wtile_bytes +
+                      (size_t)ns * a.slot_stride;
   const int grid = std::max(1, std::min(p->C, p->num_sms));
   // WorkItems computes (tail stages) x (CTA index) in 32 bits; a CTA holds at
   // most C / grid whole channels and two pieces
