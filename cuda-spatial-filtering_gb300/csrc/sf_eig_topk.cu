@@ -11,8 +11,8 @@
 //      (the published LAPACK zhetd2/zlarfg algorithm: reflectors
 //      H = I - tau v v^H, subdiagonal made real); the matrix-vector product
 //      and the rank-2 update are spread over the CTA
-//   3. eigenvalues from Sturm counts: every eigenvalue by bisection (one
-//      thread each), or only the top K by 33-way multisection (one warp each)
+//   3. eigenvalues from Sturm counts: every eigenvalue by 4-way multisection
+//      (three lanes each), or only the top K by 33-way multisection (one warp each)
 //   4. K (fixed, percentile rule of spatial.cuh:900-950, or noise floor)
 //   5. the top-K eigenvectors of T by inverse iteration (LU with partial
 //      pivoting, three iterations, modified Gram-Schmidt among them)
