@@ -42,7 +42,12 @@
 //   warp 1           TMEM allocation + the single-thread UMMA issuer
 //   warps 4-7        epilogue (one TMEM lane quarter each)
 //   warps 2-3, 8-15  converters: ring (int8) -> swizzled fp16 tiles (per-packet
-//                    scale, per-FPGA window offset); per channel the weight tile
+//                    scale, per-FPGA window offset); per channel the weight tile.
+//                    One of them (the leader) acquires each stage's packets and
+//                    operand stage ahead; another hands each written stage to
+//                    the MMA issuer and returns its packets to the producer.
+// Operand stages: three when they fit beside a packet ring deep enough to
+// prefetch a stage (the correlator), else two (the beamformer's weight tiles).
 // Every wait is bounded (about a second) and reports through the status word.
 #include <algorithm>
 #include <cstdio>
@@ -597,8 +602,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     int q_rel = 0;           // hand-off warp: first packet not yet returned to the producer
     int q_wait = 0;          // leader: first packet not yet waited for
     bool acq_ok = true;
-    // leader: wait for the packets of stage pr of the current channel and a
-    // free operand stage for op_iter_next; publish the packet flags
+    // leader: wait for the packets of stage pr of the current channel and for
+    // the operand stage of iteration `it` to be free; publish the packets'
+    // scale flags and whether the whole stage is on unit scales
     auto acquire = [&](int pr, uint32_t gq0, uint32_t it) {
       const int s0 = pr * TILE_T;
       const int qb = s0 < T ? min(a.P + 1, static_cast<int>(__umulhi(static_cast<uint32_t>(min(s0 + TILE_T - 1, T - 1) + off_max), a.tp_magic)))
