@@ -134,9 +134,13 @@ SF_DEVICE void stockham_pass(float2 *x, const __half2 *src, const float2 *tw, co
   for (int b = 0; b < PER; ++b) {
     const int j = threadIdx.x + b * BS_THREADS;
     if (NB % BS_THREADS == 0 || j < NB) {
+      // with NB a multiple of 256, r NB leaves bits 4..7 alone:
+      // bs_swz(j + r NB) = bs_swz(j) + r NB
+      const int js = bs_swz(j);
 #pragma unroll
       for (int r = 0; r < R; ++r)
-        v[b][r] = NS == 1 ? __half22float2(src[j + r * NB]) : x[bs_swz(j + r * NB)];
+        v[b][r] = NS == 1 ? __half22float2(src[j + r * NB])
+                          : x[NB % 256 == 0 ? js + r * NB : bs_swz(j + r * NB)];
     }
   }
   if (NS > 1) __syncthreads();
@@ -151,8 +155,19 @@ SF_DEVICE void stockham_pass(float2 *x, const __half2 *src, const float2 *tw, co
       }
       dft_reg<LOG2R>(v[b], w);
       const int base = (j - jm) * R + jm;
+      // the swizzle of base + k NS for the pass shapes of the radix-16 plan:
+      // NS = 1 (base a multiple of 16): bs_swz(base) ^ k; NS = R = 16 (base =
+      // 256 m + jm): (base ^ k) + 16 k; NS a multiple of 256: bs_swz(base) + k NS
+      const int bs = bs_swz(base);
 #pragma unroll
-      for (int k = 0; k < R; ++k) x[bs_swz(base + k * NS)] = v[b][bitrev(k, LOG2R)];
+      for (int k = 0; k < R; ++k) {
+        int pos;
+        if constexpr (NS == 1 && R == 16) pos = bs ^ k;
+        else if constexpr (NS == 16 && R == 16) pos = (base ^ k) + 16 * k;
+        else if constexpr (NS % 256 == 0) pos = bs + k * NS;
+        else pos = bs_swz(base + k * NS);
+        x[pos] = v[b][bitrev(k, LOG2R)];
+      }
     }
   }
   __syncthreads();
