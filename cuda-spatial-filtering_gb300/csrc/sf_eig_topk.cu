@@ -197,7 +197,8 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
     sd[i] = sqrtf(fmaxf(x.x, 1e-10f));
   }
   __syncthreads();
-  // lower triangle only (A[i][j], j <= i); the upper half is its conjugate
+  // both triangles (A[i][j] and A[j][i] = conj(A[i][j])), so that the
+  // Householder matrix-vector product reads plain rows
   for (int e0 = tid; e0 < n * n; e0 += NT) {
     const int i = e0 / n, j = e0 - (e0 / n) * n;
     if (j > i) continue;
@@ -206,6 +207,7 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
     x = cmulc(cmul(dp[j], x), dp[i]);  // element (j, i) of the upper triangle
     const float inv = 1.0f / (sd[i] * sd[j]);
     A[i * ld + j] = i == j ? make_float2(x.x * inv, 0.0f) : make_float2(x.x * inv, -x.y * inv);
+    if (j < i) A[j * ld + i] = make_float2(x.x * inv, x.y * inv);
   }
   __syncthreads();
 
@@ -221,23 +223,20 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
     const float2 tau = taus[k];
     float2 *A22 = A + (k + 1) * ld + (k + 1);
     if (tau.x != 0.0f || tau.y != 0.0f) {
-      // p = tau A22 v, A22 Hermitian held as its lower triangle: two threads
-      // per row, even / odd columns, A22[i][j] = conj(A22[j][i]) above the diagonal
+      // p = tau A22 v, A22 Hermitian held in both triangles: two threads per
+      // row, even / odd columns
       const int i = tid >> 1, h = tid & 1;
       float2 acc0 = make_float2(0.0f, 0.0f), acc1 = make_float2(0.0f, 0.0f);
       if (i < m) {
-        // row i below the diagonal, conj(column i) above it; four loads in
-        // flight before their products
+        // four loads in flight before their products
         const float2 *rowp = A22 + i * ld;
-        const float2 *colp = A22 + i;
         int j = h;
         for (; j + 6 < m; j += 8) {
           float2 x[4], vv[4];
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             const int jj = j + 2 * u;
-            const float2 raw = jj <= i ? rowp[jj] : colp[jj * ld];
-            x[u] = jj <= i ? raw : make_float2(raw.x, -raw.y);
+            x[u] = rowp[jj];
             vv[u] = vb[jj];
           }
 #pragma unroll
@@ -251,9 +250,7 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
           }
         }
         for (; j < m; j += 2) {
-          const float2 raw = j <= i ? rowp[j] : colp[j * ld];
-          const float2 x0 = j <= i ? raw : make_float2(raw.x, -raw.y);
-          const float2 t0 = cmul(x0, vb[j]);
+          const float2 t0 = cmul(rowp[j], vb[j]);
           acc0.x += t0.x;
           acc0.y += t0.y;
         }
@@ -358,7 +355,9 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
             const float2 t3 = cmulc(vi, vj);
             float2 *el = A22 + ii * ld + jj;
             const float2 old = *el;
-            *el = make_float2(old.x - t1.x - t2.x - cvv * t3.x, old.y - t1.y - t2.y - cvv * t3.y);
+            const float2 nw = make_float2(old.x - t1.x - t2.x - cvv * t3.x, old.y - t1.y - t2.y - cvv * t3.y);
+            *el = nw;
+            if (jj != ii) A22[jj * ld + ii] = make_float2(nw.x, -nw.y);  // the upper triangle
           }
         }
       }
