@@ -189,41 +189,64 @@ __global__ void __launch_bounds__(BS_THREADS) sf_beam_spectra_kernel(const BeamS
   const int s = blockIdx.x;
   stockham_fft<T, 1>(xs, a.beams + (size_t)s * T, a.tw, a.w);
 
+  // |X|^2 >= 0 (or +inf), so a group's plain sum is NaN exactly when one of
+  // its bins is: the plain sum serves every group without NaN bins (same
+  // order, same count D), and only a NaN sum takes the NaN-skipping mean
   const int D = a.D, G = T / D;
   float *out = a.out + (size_t)s * G;
   if (D >= 32) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int g = warp; g < G; g += BS_THREADS / 32) {
       float sum = 0.f;
-      int cnt = 0;
       for (int i = lane; i < D; i += 32) {
         const float2 X = xs[bs_swz(g * D + i)];
-        const float pw = X.x * X.x + X.y * X.y;
-        if (!isnan(pw)) {
-          sum += pw;
-          ++cnt;
-        }
+        sum += X.x * X.x + X.y * X.y;
       }
 #pragma unroll
-      for (int o = 16; o; o >>= 1) {
-        sum += __shfl_xor_sync(0xffffffffu, sum, o);
-        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+      for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      if (isnan(sum)) {  // warp-uniform after the reduction
+        sum = 0.f;
+        int cnt = 0;
+        for (int i = lane; i < D; i += 32) {
+          const float2 X = xs[bs_swz(g * D + i)];
+          const float pw = X.x * X.x + X.y * X.y;
+          if (!isnan(pw)) {
+            sum += pw;
+            ++cnt;
+          }
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+          sum += __shfl_xor_sync(0xffffffffu, sum, o);
+          cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        }
+        if (lane == 0) out[g] = cnt > 0 ? sum / (float)cnt : 0.f;
+      } else if (lane == 0) {
+        out[g] = sum / (float)D;
       }
-      if (lane == 0) out[g] = cnt > 0 ? sum / (float)cnt : 0.f;
     }
   } else {
     for (int g = threadIdx.x; g < G; g += BS_THREADS) {
       float sum = 0.f;
-      int cnt = 0;
       for (int i = 0; i < D; ++i) {
         const float2 X = xs[bs_swz(g * D + i)];
-        const float pw = X.x * X.x + X.y * X.y;
-        if (!isnan(pw)) {
-          sum += pw;
-          ++cnt;
-        }
+        sum += X.x * X.x + X.y * X.y;
       }
-      out[g] = cnt > 0 ? sum / (float)cnt : 0.f;
+      if (isnan(sum)) {
+        sum = 0.f;
+        int cnt = 0;
+        for (int i = 0; i < D; ++i) {
+          const float2 X = xs[bs_swz(g * D + i)];
+          const float pw = X.x * X.x + X.y * X.y;
+          if (!isnan(pw)) {
+            sum += pw;
+            ++cnt;
+          }
+        }
+        out[g] = cnt > 0 ? sum / (float)cnt : 0.f;
+      } else {
+        out[g] = sum / (float)D;
+      }
     }
   }
 }
