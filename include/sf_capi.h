@@ -213,7 +213,11 @@ int sf_packet_spectra(sf_plan *plan, const uint16_t *d_beams_f16, int32_t n_beam
 
 /* ---- whole chains (what the drop-in pipelines run per buffer) -------------- */
 
-/* LambdaCorrBeamOnlyGPUPipeline::enqueue_main (lambda_corr_beam_only_gpu_pipeline.hpp:305-344). */
+/* LambdaCorrBeamOnlyGPUPipeline::enqueue_main (lambda_corr_beam_only_gpu_pipeline.hpp:305-344).
+ * One pass over the samples yields visibilities and beams when the fused
+ * tensor-memory layout fits (4R + the beam columns; not at R = 48) and
+ * d_samples is 16-byte aligned; otherwise a correlation and a beamforming
+ * launch give the same outputs.  The same holds for sf_run_lambda_gpu. */
 int sf_run_corr_beam(sf_plan *plan, const int8_t *d_samples, const int16_t *d_scales,
                      int32_t *d_vis, uint16_t *d_beams_f16, void *stream);
 
