@@ -18,13 +18,15 @@
 #endif
 
 // Bits written into the per-plan device status word (sf_plan_status reads it).
+// (the public names and meanings are sf_device_bits in sf_capi.h)
 enum : uint32_t {
-  SF_DEVERR_TIMEOUT_TMA = 1u << 0,
-  SF_DEVERR_TIMEOUT_CONVERT = 1u << 1,
-  SF_DEVERR_TIMEOUT_MMA = 1u << 2,
-  SF_DEVERR_TIMEOUT_EPILOGUE = 1u << 3,
-  SF_DEVERR_EIG_NOT_CONVERGED = 1u << 4,
-  SF_DEVERR_BAD_SHAPE = 1u << 5,
+  SF_DEVERR_TIMEOUT_TMA = SF_DEV_TIMEOUT_TMA,
+  SF_DEVERR_TIMEOUT_CONVERT = SF_DEV_TIMEOUT_CONVERT,
+  SF_DEVERR_TIMEOUT_MMA = SF_DEV_TIMEOUT_MMA,
+  SF_DEVERR_TIMEOUT_EPILOGUE = SF_DEV_TIMEOUT_EPILOGUE,
+  SF_DEVERR_EIG_NOT_CONVERGED = SF_DEV_EIG_NOT_CONVERGED,
+  SF_DEVERR_BAD_SHAPE = SF_DEV_BAD_SHAPE,
+  SF_DEVERR_BAD_DELAY = SF_DEV_BAD_DELAY,
 };
 
 // ---------------------------------------------------------------------------

@@ -924,18 +924,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
   }
 }
 
-int g_max_smem = 0;
-bool g_attr_set[8] = {false, false, false, false, false, false, false, false};
-
 template <bool DO_CORR, bool DO_BEAM, bool CORNER>
 cudaError_t launch_mode(const CorrArgs &a, size_t smem, int grid, cudaStream_t stream) {
-  const int idx = (DO_CORR ? 1 : 0) + (DO_BEAM ? 2 : 0) + (CORNER ? 4 : 0);
-  if (!g_attr_set[idx]) {
-    cudaError_t e = cudaFuncSetAttribute(sf_corrbeam_kernel<DO_CORR, DO_BEAM, CORNER>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, g_max_smem);
-    if (e != cudaSuccess) return e;
-    g_attr_set[idx] = true;
-  }
+  cudaError_t e = sf_smem_optin(reinterpret_cast<const void *>(sf_corrbeam_kernel<DO_CORR, DO_BEAM, CORNER>), smem);
+  if (e != cudaSuccess) return e;
   sf_corrbeam_kernel<DO_CORR, DO_BEAM, CORNER><<<grid, NTHREADS, smem, stream>>>(a);
   return cudaGetLastError();
 }
@@ -1039,18 +1031,14 @@ cudaError_t sf_launch_corrbeam(const sf_plan *p, const int8_t *samples, const in
   }
   if (a.tmem_cols > 512) return cudaErrorInvalidConfiguration;
 
-  if (!g_max_smem) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  }
+  const int max_smem = sf_device_max_smem();
   // packets one stage touches: (TILE_T - 1 + window spread <= 2 Tp) / Tp + 2, plus one in flight
   const int need_slots = (TILE_T - 1) / p->Tp + 5;
   const int prefetch_slots = (2 * TILE_T - 1) / p->Tp + 5;
   // ring depth beside `stages` operand stages (a power of two)
   auto ring_depth = [&](int stages) {
     const long fixed = HEADER_BYTES + 1024 + (long)stages * a.natoms * ATOM_BYTES + 2 * (long)a.wtile_bytes;
-    const long avail = (long)g_max_smem - fixed;
+    const long avail = (long)max_smem - fixed;
     int ns = avail > 0 ? (int)std::min<long>(MAX_SLOTS, avail / a.slot_stride) : 0;
     while (ns & (ns - 1)) ns &= ns - 1;  // round down to a power of two
     return ns;

@@ -419,13 +419,8 @@ cudaError_t sf_launch_eig(const sf_plan *p, const int32_t *vis, int eig_mode, in
   const int np = (p->R + 1) & ~1;
   const size_t smem = (size_t)2 * np * (np + 1) * sizeof(float2) + (size_t)(np / 2) * sizeof(Rot) +
                       (size_t)np * (2 * sizeof(float) + sizeof(int));
-  static int attr_done = 0;
-  if (!attr_done) {
-    cudaError_t e = cudaFuncSetAttribute(sf_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         96 * 1024);
-    if (e != cudaSuccess) return e;
-    attr_done = 1;
-  }
+  cudaError_t e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_kernel), smem);
+  if (e != cudaSuccess) return e;
   const int batch = eig_mode == SF_EIG_ALL_BLOCKS ? p->C * 4 : p->C * 2;
   sf_eig_kernel<<<batch, EIG_THREADS, smem, stream>>>(a);
   return cudaGetLastError();

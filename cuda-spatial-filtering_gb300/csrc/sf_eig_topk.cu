@@ -717,13 +717,8 @@ cudaError_t sf_launch_eig_topk(const sf_plan *p, const int32_t *vis, int k_rule,
   a.shrink = shrink;
   a.delta = delta;
   const size_t smem = sf_eig_topk_smem(p->R, p->B);
-  static int attr_done = 0;
-  if (!attr_done) {
-    cudaError_t e = cudaFuncSetAttribute(sf_eig_topk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         200 * 1024);
-    if (e != cudaSuccess) return e;
-    attr_done = 1;
-  }
+  cudaError_t e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel), smem);
+  if (e != cudaSuccess) return e;
   sf_eig_topk_kernel<<<p->C * 2, NT, smem, stream>>>(a);
   return cudaGetLastError();
 }

@@ -14,9 +14,11 @@
 // holds until the process exits.  It stores the window offsets, the
 // per-receiver factors, the fixed counts, the visibilities, the effective
 // weights, the counts (when the caller passes none) and the status word.
-// The first call on each device looks the array's device address up with
-// cudaGetSymbolAddress (with that device current) and caches it, so make
-// that first call before any stream capture.  All calls on a device share
+// The first call on each device is the set-up call: it looks the array's
+// device address up with cudaGetSymbolAddress (with that device current) and
+// caches it.  That lookup may load the library's device code and commit the
+// 16 MiB, so make the first call outside the real-time path and before any
+// stream capture; later calls allocate nothing.  All calls on a device share
 // its one array, which keeps the last call's contents: calls that overlap on
 // the same GPU (for example on two streams) race with each other, so the
 // caller must serialise them (one stream, or events between streams).
@@ -40,19 +42,35 @@ std::mutex g_scratch_mu;
 size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Per-call state that must start fresh: window offsets, factors, fixed
-// counts and the status word.  Visibilities and effective weights are fully
-// rewritten by the kernels of every call.
+// counts and the scratch status word.  Visibilities and effective weights are
+// fully rewritten by the kernels of every call.  The correlator's packet ring
+// and the beamformer's sample index assume window offsets in [0, 2 Tp], so a
+// delay outside [-Tp, Tp] is replaced by 0 and reported (SF_DEVERR_BAD_DELAY)
+// instead of letting a kernel read outside the caller's samples.  Thread 0
+// clears the scratch status before it reports, so the two cannot race when
+// the report goes to the scratch word.
 __global__ void sf_noalloc_init_kernel(int32_t *offsets, const int32_t *delays, int F, int Tp,
                                        float2 *factors, const float2 *factors_in, int nfactors,
                                        int32_t *fixed, const int32_t *fixed_in, int C,
-                                       uint32_t *status) {
+                                       uint32_t *scratch_status, uint32_t *report_status) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int stride = gridDim.x * blockDim.x;
-  for (int f = tid; f < F; f += stride) offsets[f] = Tp + (delays ? delays[f] : 0);
+  if (tid == 0) {
+    *scratch_status = 0;
+    bool bad = false;
+    for (int f = 0; f < F; ++f) {
+      int d = delays ? delays[f] : 0;
+      if (d < -Tp || d > Tp) {
+        bad = true;
+        d = 0;
+      }
+      offsets[f] = Tp + d;
+    }
+    if (bad) atomicOr(report_status, SF_DEVERR_BAD_DELAY);
+  }
   for (int i = tid; i < nfactors; i += stride)
     factors[i] = factors_in ? factors_in[i] : make_float2(1.0f, 0.0f);
   for (int c = tid; c < C; c += stride) fixed[c] = fixed_in ? fixed_in[c] : 0;
-  if (tid == 0) *status = 0;
 }
 
 }  // namespace
@@ -79,6 +97,10 @@ extern "C" int sf_run_adaptive_noalloc(const sf_shape *shape, const int8_t *d_sa
     return sf_internal_set_error(SF_ERR_INVALID_ARGUMENT, "unknown K rule");
   if (reinterpret_cast<uintptr_t>(d_samples) % 16 != 0)
     return sf_internal_set_error(SF_ERR_INVALID_ARGUMENT, "samples must be 16-byte aligned");
+  if (reinterpret_cast<uintptr_t>(d_factors) % 8 != 0)
+    return sf_internal_set_error(SF_ERR_INVALID_ARGUMENT, "factors must be 8-byte aligned");
+  if (reinterpret_cast<uintptr_t>(d_weights_f16) % 4 != 0 || reinterpret_cast<uintptr_t>(d_beams_f16) % 4 != 0)
+    return sf_internal_set_error(SF_ERR_INVALID_ARGUMENT, "weights and beams must be 4-byte aligned");
 
   // A plan-shaped view over the caller's buffers and the static scratch:
   // built on the stack, nothing allocated.
@@ -157,7 +179,7 @@ extern "C" int sf_run_adaptive_noalloc(const sf_shape *shape, const int8_t *d_sa
                                             reinterpret_cast<const float2 *>(d_factors),
                                             static_cast<int>(C * 2 * R), p.d_fixed_counts,
                                             d_fixed_counts, p.C,
-                                            reinterpret_cast<uint32_t *>(base + off_status));
+                                            reinterpret_cast<uint32_t *>(base + off_status), p.d_status);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = sf_launch_correlate(&p, d_samples, d_scales, p.d_off_aligned, p.d_vis, st);
   if (e == cudaSuccess)
@@ -166,6 +188,8 @@ extern "C" int sf_run_adaptive_noalloc(const sf_shape *shape, const int8_t *d_sa
   if (e == cudaSuccess)
     e = sf_launch_beam(&p, d_samples, d_scales, p.d_off_aligned, 2,
                        reinterpret_cast<__half2 *>(d_beams_f16), st);
+  if (e == cudaErrorInvalidConfiguration)
+    return sf_internal_set_error(SF_ERR_UNSUPPORTED, "packet ring does not fit shared memory for this shape");
   if (e != cudaSuccess) {
     snprintf(msg, sizeof(msg), "allocation-free chain launch: %s", cudaGetErrorString(e));
     return sf_internal_set_error(SF_ERR_CUDA, msg);

@@ -590,23 +590,15 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return fn;
 }
 
-constexpr int MAX_DEVICES = 64;
-bool g_bs_attr[MAX_DEVICES][BS_MAX_LOG2T + 1];
-bool g_pk_attr[MAX_DEVICES][7];
-bool g_tc_attr[MAX_DEVICES];
-
 template <typename K>
-cudaError_t ensure_smem(K kernel, bool &done, size_t smem) {
-  if (done || smem <= 48 * 1024) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e == cudaSuccess) done = true;
-  return e;
+cudaError_t ensure_smem(K kernel, size_t smem) {
+  return sf_smem_optin(reinterpret_cast<const void *>(kernel), smem);
 }
 
 template <int LOG2T>
 cudaError_t launch_bs(const BeamSpecArgs &a, int dev, cudaStream_t stream) {
   const size_t smem = sizeof(float2) << LOG2T;
-  cudaError_t e = ensure_smem(sf_beam_spectra_kernel<LOG2T>, g_bs_attr[dev][LOG2T], smem);
+  cudaError_t e = ensure_smem(sf_beam_spectra_kernel<LOG2T>, smem);
   if (e != cudaSuccess) return e;
   sf_beam_spectra_kernel<LOG2T><<<a.S, BS_THREADS, smem, stream>>>(a);
   return cudaGetLastError();
@@ -615,7 +607,7 @@ cudaError_t launch_bs(const BeamSpecArgs &a, int dev, cudaStream_t stream) {
 template <int LOG2TP>
 cudaError_t launch_pk(const PacketSpecArgs &a, int dev, cudaStream_t stream) {
   const size_t smem = (size_t)PK_WARPS * 2 * PK_CHUNK * (1 << LOG2TP) * 4;
-  cudaError_t e = ensure_smem(sf_packet_spectra_kernel<LOG2TP>, g_pk_attr[dev][LOG2TP], smem);
+  cudaError_t e = ensure_smem(sf_packet_spectra_kernel<LOG2TP>, smem);
   if (e != cudaSuccess) return e;
   sf_packet_spectra_kernel<LOG2TP><<<(a.S + PK_WARPS - 1) / PK_WARPS, PK_WARPS * 32, smem, stream>>>(a);
   return cudaGetLastError();
@@ -669,7 +661,6 @@ cudaError_t sf_launch_beam_spectra(const sf_plan *p, const __half2 *beams, int n
   a.S = p->C * 2 * n_beams_out;
   a.D = downsample;
   a.w = tw64();
-  if (p->device < 0 || p->device >= MAX_DEVICES) return cudaErrorInvalidDevice;
   switch (log2_exact(p->T)) {
     case 6: return launch_bs<6>(a, p->device, stream);
     case 7: return launch_bs<7>(a, p->device, stream);
@@ -736,9 +727,8 @@ cudaError_t sf_launch_packet_spectra(const sf_plan *p, const __half2 *beams, int
     a.S = S;
     a.P = p->P;
     a.trim = trim;
-    if (p->device < 0 || p->device >= MAX_DEVICES) return cudaErrorInvalidDevice;
     const size_t smem = tc_smem_bytes();
-    cudaError_t e = ensure_smem(sf_packet_spectra_tc_kernel, g_tc_attr[p->device], smem);
+    cudaError_t e = ensure_smem(sf_packet_spectra_tc_kernel, smem);
     if (e != cudaSuccess) return e;
     const int grid = S < p->num_sms ? S : p->num_sms;
     sf_packet_spectra_tc_kernel<<<grid, TC_THREADS, smem, stream>>>(tmap, a);
@@ -751,7 +741,6 @@ cudaError_t sf_launch_packet_spectra(const sf_plan *p, const __half2 *beams, int
   a.P = p->P;
   a.trim = trim;
   a.w = tw64();
-  if (p->device < 0 || p->device >= MAX_DEVICES) return cudaErrorInvalidDevice;
   switch (log2_exact(p->Tp)) {
     case 4: return launch_pk<4>(a, p->device, stream);
     case 5: return launch_pk<5>(a, p->device, stream);

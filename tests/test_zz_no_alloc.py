@@ -94,3 +94,61 @@ def test_noalloc_rejects_shapes_beyond_its_scratch():
     with pytest.raises(sfgb.SfError) as ei:
         sfgb.run_adaptive_noalloc(big, s, sc, w, sfgb.SF_K_FIXED, 0.0, False, beams)
     assert ei.value.code == 2 and "scratch" in str(ei.value)
+
+
+def test_noalloc_second_call_allocates_nothing():
+    # The first call on a device is the set-up call (it resolves the static
+    # array's address); after it, a call must leave both the device's free
+    # memory and torch's allocator untouched.
+    args = _inputs(3)
+    sh, samples, scales, weights, gains, delays, fixed = args
+    s = torch.as_tensor(samples).cuda()
+    sc = torch.as_tensor(scales).cuda()
+    w = torch.as_tensor(np.ascontiguousarray(weights)).cuda()
+    beams = torch.empty((sh.C, 2, 2 * sh.B, sh.T, 2), dtype=torch.float16, device="cuda")
+    cnt = torch.empty((sh.C, 2), dtype=torch.int32, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    call = lambda: sfgb.run_adaptive_noalloc(SHAPE, s, sc, w, sfgb.SF_K_FIXED, 0.0, False, beams,
+                                             counts=cnt, status=status)
+    call()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    alloc0 = torch.cuda.memory_allocated()
+    call()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert torch.cuda.memory_allocated() == alloc0
+    assert free1 == free0
+    assert int(status.item()) == 0
+
+
+def test_noalloc_out_of_range_delay_is_replaced_and_reported():
+    # A delay outside [-Tp, Tp] would move the sample window outside the
+    # caller's buffer: the entry point replaces it by 0 and raises the
+    # SF_DEV_BAD_DELAY bit, and the beams equal those of a zero delay.
+    sh, samples, scales, weights, gains, delays, fixed = _inputs(4)
+    bad = np.zeros(sh.F, np.int32)
+    bad[1] = 3 * sh.Tp
+    bad[2] = -2 * sh.Tp - 5
+    got_beams, got_counts, bits = _noalloc_with_delays(sh, samples, scales, weights, bad)
+    assert bits & sfgb.SF_DEV_BAD_DELAY
+    ref_beams, ref_counts, ref_bits = _noalloc_with_delays(sh, samples, scales, weights, np.zeros(sh.F, np.int32))
+    assert ref_bits == 0
+    assert np.all(np.isfinite(got_beams))
+    assert np.array_equal(got_counts, ref_counts)
+    assert np.array_equal(got_beams, ref_beams)
+
+
+def _noalloc_with_delays(sh, samples, scales, weights, delays):
+    s = torch.as_tensor(samples).cuda()
+    sc = torch.as_tensor(scales).cuda()
+    w = torch.as_tensor(np.ascontiguousarray(weights)).cuda()
+    dl = torch.as_tensor(delays).cuda()
+    fx = torch.ones(sh.C, dtype=torch.int32, device="cuda")
+    beams = torch.full((sh.C, 2, 2 * sh.B, sh.T, 2), float("nan"), dtype=torch.float16, device="cuda")
+    cnt = torch.full((sh.C, 2), -1, dtype=torch.int32, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    sfgb.run_adaptive_noalloc(SHAPE, s, sc, w, sfgb.SF_K_FIXED, 0.0, False, beams, delays=dl,
+                              fixed_counts=fx, counts=cnt, status=status)
+    torch.cuda.synchronize()
+    return beams.cpu().numpy().astype(np.float32), cnt.cpu().numpy(), int(status.item())
