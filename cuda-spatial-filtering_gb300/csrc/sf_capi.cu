@@ -6,7 +6,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
+#include <vector>
 
 #include "sf_common.cuh"
 #include "sf_plan.cuh"
@@ -53,8 +55,13 @@ void free_plan(sf_plan *p) {
   cudaFree(p->d_steer);
   cudaFree(p->d_steer_conn);
   cudaFree(p->d_steer_cal);
-  free(p->h_steer);
-  free(p->h_steer_conn);
+  if (p->steer_uploaded) {
+    cudaEventSynchronize(p->steer_uploaded);
+    cudaEventDestroy(p->steer_uploaded);
+  }
+  cudaFreeHost(p->h_steer);
+  cudaFreeHost(p->h_steer_conn);
+  cudaFreeHost(p->h_steer_cal);
   cudaFree(p->d_fixed_counts);
   cudaFree(p->d_vis);
   cudaFree(p->d_evals);
@@ -103,6 +110,44 @@ int upload_offsets(sf_plan *p, cudaStream_t s) {
 }
 
 }  // namespace
+
+namespace {
+struct SmemOptin {
+  int device;
+  const void *func;
+  size_t bytes;
+};
+std::mutex g_optin_mu;
+std::vector<SmemOptin> g_optin;
+constexpr int MAX_DEVICES = 64;
+int g_max_smem[MAX_DEVICES];
+}  // namespace
+
+cudaError_t sf_smem_optin(const void *func, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(g_optin_mu);
+  for (SmemOptin &o : g_optin)
+    if (o.device == dev && o.func == func) {
+      if (o.bytes >= bytes) return cudaSuccess;
+      e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+      if (e == cudaSuccess) o.bytes = bytes;
+      return e;
+    }
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+  if (e == cudaSuccess) g_optin.push_back({dev, func, bytes});
+  return e;
+}
+
+int sf_device_max_smem() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return 0;
+  std::lock_guard<std::mutex> lock(g_optin_mu);
+  if (!g_max_smem[dev]) cudaDeviceGetAttribute(&g_max_smem[dev], cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return g_max_smem[dev];
+}
 
 // Lets other translation units of the library report through sf_last_error.
 int sf_internal_set_error(int code, const char *msg) { return set_err(code, "%s", msg); }
@@ -155,10 +200,7 @@ int sf_plan_create(const sf_shape *shape, sf_plan **out_plan) {
   p->h_phasors = static_cast<float2 *>(malloc(sizeof(float2) * C * R));
   p->h_factors = static_cast<float2 *>(malloc(sizeof(float2) * C * 2 * R));
   p->h_fixed_counts = static_cast<int32_t *>(calloc(C, sizeof(int32_t)));
-  p->h_steer = static_cast<double *>(calloc(3 * (B + R), sizeof(double)));
-  p->h_steer_conn = static_cast<int32_t *>(calloc(R, sizeof(int32_t)));
-  if (!p->h_delays || !p->h_gains || !p->h_phasors || !p->h_factors || !p->h_fixed_counts || !p->h_steer ||
-      !p->h_steer_conn) {
+  if (!p->h_delays || !p->h_gains || !p->h_phasors || !p->h_factors || !p->h_fixed_counts) {
     free_plan(p);
     return set_err(SF_ERR_INVALID_ARGUMENT, "out of host memory");
   }
@@ -189,6 +231,16 @@ int sf_plan_create(const sf_shape *shape, sf_plan **out_plan) {
   SF_ALLOC(p->d_steer_conn, sizeof(int32_t) * R);
   SF_ALLOC(p->d_steer_cal, sizeof(float2) * C * 2 * R);
 #undef SF_ALLOC
+  {
+    cudaError_t eh = cudaMallocHost(reinterpret_cast<void **>(&p->h_steer), sizeof(double) * 3 * (B + R));
+    if (eh == cudaSuccess) eh = cudaMallocHost(reinterpret_cast<void **>(&p->h_steer_conn), sizeof(int32_t) * R);
+    if (eh == cudaSuccess) eh = cudaMallocHost(reinterpret_cast<void **>(&p->h_steer_cal), sizeof(float2) * C * 2 * R);
+    if (eh == cudaSuccess) eh = cudaEventCreateWithFlags(&p->steer_uploaded, cudaEventDisableTiming);
+    if (eh != cudaSuccess) {
+      free_plan(p);
+      return cuda_err(eh, "pinned steering staging");
+    }
+  }
   cudaError_t ez = cudaSuccess;
   ez = ez != cudaSuccess ? ez : cudaMemset(p->d_off_packet, 0, sizeof(int32_t) * p->F);
   ez = ez != cudaSuccess ? ez : cudaMemset(p->d_weights, 0, sizeof(__half2) * C * 2 * B * R);
@@ -340,22 +392,36 @@ int sf_set_steering_weights(sf_plan *plan, const double *h_dircos, const double 
     if (!std::isfinite(h_enu[i])) return set_err(SF_ERR_INVALID_ARGUMENT, "antenna coordinate %d is not finite", i);
   if (!std::isfinite(base_freq_hz) || !std::isfinite(channel_bw_hz))
     return set_err(SF_ERR_INVALID_ARGUMENT, "frequency plan is not finite");
-  // stage in plan-owned host memory: the caller's arrays are free on return
+  // Stage in the plan's pinned buffers (the caller's arrays are free on
+  // return) once the previous refresh's copies out of them have landed --
+  // that waits for those copies only, never for the runs queued on `stream`.
+  SF_TRY(cudaEventSynchronize(plan->steer_uploaded), "previous steering upload");
   memcpy(plan->h_steer, h_dircos, sizeof(double) * 3 * B);
   memcpy(plan->h_steer + 3 * B, h_enu, sizeof(double) * 3 * R);
   for (int r = 0; r < R; ++r) plan->h_steer_conn[r] = h_connected ? (h_connected[r] != 0) : 1;
+  if (h_cal_gains) memcpy(plan->h_steer_cal, h_cal_gains, sizeof(float2) * plan->C * 2 * R);
   cudaStream_t s = as_stream(stream);
   SF_TRY(cudaMemcpyAsync(plan->d_steer, plan->h_steer, sizeof(double) * 3 * (B + R), cudaMemcpyHostToDevice, s),
          "steering upload");
   SF_TRY(cudaMemcpyAsync(plan->d_steer_conn, plan->h_steer_conn, sizeof(int32_t) * R, cudaMemcpyHostToDevice, s),
          "steering upload");
   if (h_cal_gains)
-    SF_TRY(cudaMemcpyAsync(plan->d_steer_cal, h_cal_gains, sizeof(float2) * plan->C * 2 * R, cudaMemcpyHostToDevice, s),
+    SF_TRY(cudaMemcpyAsync(plan->d_steer_cal, plan->h_steer_cal, sizeof(float2) * plan->C * 2 * R,
+                           cudaMemcpyHostToDevice, s),
            "calibration upload");
+  SF_TRY(cudaEventRecord(plan->steer_uploaded, s), "steering upload event");
+  // the synthesis writes the weights in stream order: runs queued before it
+  // finish on the old weights, runs queued after it read the new ones
   SF_TRY(sf_launch_steering(plan, plan->d_steer, plan->d_steer + 3 * B, plan->d_steer_conn,
                             h_cal_gains ? plan->d_steer_cal : nullptr, base_freq_hz, channel_bw_hz, min_freq_ch, s),
          "steering launch");
-  SF_TRY(cudaStreamSynchronize(s), "steering synthesis");
+  return SF_OK;
+}
+
+int sf_plan_weights_buffer(sf_plan *plan, void **out_device_weights) {
+  if (int rc = check_plan(plan)) return rc;
+  if (!out_device_weights) return set_err(SF_ERR_INVALID_ARGUMENT, "out pointer is NULL");
+  *out_device_weights = plan->d_weights;
   return SF_OK;
 }
 
@@ -408,6 +474,15 @@ int sf_covariance_eig(sf_plan *plan, const int32_t *d_vis, int32_t eig_mode, int
                        reinterpret_cast<float2 *>(d_evecs), d_counts,
                        reinterpret_cast<__half2 *>(d_proj_f16), as_stream(stream)),
          "eig launch");
+  return SF_OK;
+}
+
+int sf_get_effective_weights(sf_plan *plan, float *d_weff, void *stream) {
+  if (int rc = check_plan(plan)) return rc;
+  if (!d_weff) return set_err(SF_ERR_INVALID_ARGUMENT, "weff is NULL");
+  SF_TRY(cudaMemcpyAsync(d_weff, plan->d_weff, sizeof(float2) * plan->C * 2 * 2 * plan->B * plan->R,
+                         cudaMemcpyDeviceToDevice, as_stream(stream)),
+         "effective weights copy");
   return SF_OK;
 }
 

@@ -47,8 +47,12 @@ struct sf_plan {
   double *d_steer;
   int32_t *d_steer_conn;
   float2 *d_steer_cal;
+  // pinned staging of the same (so the upload is asynchronous) and the event
+  // that marks the last upload's copies done (the staging is reused after it)
   double *h_steer;
   int32_t *h_steer_conn;
+  float2 *h_steer_cal;
+  cudaEvent_t steer_uploaded;
 
   // Scratch for the whole-chain entry points.
   int32_t *d_vis;      // [C][NBL][2][2][2]
@@ -56,6 +60,14 @@ struct sf_plan {
   int32_t *d_counts;   // [C][2]
   uint32_t *d_status;  // error bits
 };
+
+// Opts `func` in to `bytes` of dynamic shared memory on the current device.
+// The attribute is per device, so the helper remembers (device, kernel,
+// bytes) under a mutex and calls cudaFuncSetAttribute once per device and
+// kernel (again only for a larger size).  Thread-safe.
+cudaError_t sf_smem_optin(const void *func, size_t bytes);
+// The current device's opt-in shared-memory limit per block (cached per device).
+int sf_device_max_smem();
 
 // Launchers (one per translation unit); each returns a cudaError_t.
 cudaError_t sf_launch_correlate(const sf_plan *p, const int8_t *samples, const int16_t *scales,

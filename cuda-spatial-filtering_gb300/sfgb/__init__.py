@@ -31,6 +31,14 @@ SF_EIG_SAME_POL_WHITENED = 1
 SF_K_FIXED = 0
 SF_K_DETECT = 1
 SF_K_NOISE_FLOOR = 2
+# device status bits (sf_device_bits)
+SF_DEV_TIMEOUT_TMA = 1 << 0
+SF_DEV_TIMEOUT_CONVERT = 1 << 1
+SF_DEV_TIMEOUT_MMA = 1 << 2
+SF_DEV_TIMEOUT_EPILOGUE = 1 << 3
+SF_DEV_EIG_NOT_CONVERGED = 1 << 4
+SF_DEV_BAD_SHAPE = 1 << 5
+SF_DEV_BAD_DELAY = 1 << 6
 
 
 class SfError(RuntimeError):
@@ -60,11 +68,13 @@ _SIGS = {
     "sf_set_fine_delays": ([_P, _P, ctypes.c_double, ctypes.c_double, _I32, _P], ctypes.c_int),
     "sf_set_weights": ([_P, _P, _P], ctypes.c_int),
     "sf_set_fixed_counts": ([_P, _P, _P], ctypes.c_int),
+    "sf_plan_weights_buffer": ([_P, ctypes.POINTER(_P)], ctypes.c_int),
     "sf_set_steering_weights": ([_P, _P, _P, _P, ctypes.c_double, ctypes.c_double, _I32, _P, _P], ctypes.c_int),
     "sf_set_stream_permutation": ([_P, _P, _P, _P], ctypes.c_int),
     "sf_correlate": ([_P, _P, _P, _I32, _P, _P], ctypes.c_int),
     "sf_covariance_eig": ([_P, _P, _I32, _I32, ctypes.c_float, _I32, _P, _P, _P, _P, _P], ctypes.c_int),
     "sf_beamform": ([_P, _P, _P, _I32, _I32, _P, _P], ctypes.c_int),
+    "sf_get_effective_weights": ([_P, _P, _P], ctypes.c_int),
     "sf_accumulate_visibilities": ([_P, _P, _P, _P], ctypes.c_int),
     "sf_visibilities_to_float": ([_P, _P, _P, _P], ctypes.c_int),
     "sf_beam_spectra": ([_P, _P, _I32, _I32, _P, _P], ctypes.c_int),
@@ -242,6 +252,11 @@ class Plan:
         _check(lib().sf_covariance_eig(self._h, _ptr(vis), int(eig_mode), int(k_rule), float(delta),
                                        int(bool(shrink)), _ptr(evals), _ptr(evecs), _ptr(counts),
                                        _ptr(proj), _stream(stream)))
+
+    def effective_weights(self, out, stream=None):
+        """Copy the plan's (original, projected) effective weights into ``out``
+        (float32 [C][2][2B][R][2] device tensor)."""
+        _check(lib().sf_get_effective_weights(self._h, _ptr(out), _stream(stream)))
 
     def beamform(self, samples, scales, window, n_slots, beams, stream=None):
         _check(lib().sf_beamform(self._h, _ptr(samples), _ptr(scales), int(window), int(n_slots),

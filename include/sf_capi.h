@@ -41,6 +41,18 @@ typedef enum sf_status {
   SF_ERR_NO_DEVICE = 5         /* no usable sm_103a device */
 } sf_status;
 
+/* Device error bits, OR-ed into a plan's status word (sf_plan_status) or the
+ * caller's status word (sf_run_adaptive_noalloc). */
+typedef enum sf_device_bits {
+  SF_DEV_TIMEOUT_TMA = 1 << 0,       /* a packet copy never landed (bounded wait ran out) */
+  SF_DEV_TIMEOUT_CONVERT = 1 << 1,   /* an operand-tile hand-off wait ran out */
+  SF_DEV_TIMEOUT_MMA = 1 << 2,       /* a tensor-core wait ran out */
+  SF_DEV_TIMEOUT_EPILOGUE = 1 << 3,  /* an accumulator drain wait ran out */
+  SF_DEV_EIG_NOT_CONVERGED = 1 << 4, /* an eigensolver hit its sweep limit */
+  SF_DEV_BAD_SHAPE = 1 << 5,         /* a kernel met a shape it does not implement */
+  SF_DEV_BAD_DELAY = 1 << 6          /* a sub-packet delay outside [-Tp, Tp] was replaced by 0 */
+} sf_device_bits;
+
 /* Integration window inside the (P+2)-packet buffer. */
 typedef enum sf_window {
   /* packets 0..P-1, no delay: LambdaCorrBeamOnlyGPUPipeline
@@ -138,10 +150,20 @@ int sf_set_weights(sf_plan *plan, const uint16_t *h_weights_f16, void *stream);
  *   h_enu        double [R][3]        position (east, north, up; metres) of each receiver's antenna
  *   h_connected  int32  [R]           0 = null input (no antenna on the stream); NULL = all connected
  *   h_cal_gains  float  [C][Pol][R][2] calibration gains G, or NULL for 1
- * Blocks until the weights are written; the host arrays are free on return. */
+ * Asynchronous, like the reference's refresh ("no GPU sync"): the host arrays are staged in the plan's
+ * pinned memory before return (they are free on return) and the synthesis runs on `stream`, so runs
+ * queued earlier on that stream finish on the old weights and later runs read the new ones.  A call
+ * waits only for the previous call's staging copies to have landed, never for queued runs. */
 int sf_set_steering_weights(sf_plan *plan, const double *h_dircos, const double *h_enu, const int32_t *h_connected,
                             double base_freq_hz, double channel_bw_hz, int32_t min_freq_ch, const float *h_cal_gains,
                             void *stream);
+
+/* Device address of the plan's beam weights, laid out as the BeamWeightsT<T> payload
+ * (fp16 pairs [C][Pol][B][R][2]), for a host steering object that enqueues its own
+ * asynchronous copies into it on the plan's stream: the reference's
+ * BeamSteering<T>::register_buffer(device_weights, stream) (reference
+ * include/spatial/pipeline/common.hpp:245-250, 296-303).  Valid until sf_plan_destroy. */
+int sf_plan_weights_buffer(sf_plan *plan, void **out_device_weights);
 
 /* Fixed K per channel (the -e map of the adaptive pipeline,
  * lambda_adaptive_beamformed_spectra_pipeline.hpp:1160-1167); NULL resets to 0. */
@@ -170,6 +192,14 @@ int sf_correlate(sf_plan *plan, const int8_t *d_samples, const int16_t *d_scales
 int sf_covariance_eig(sf_plan *plan, const int32_t *d_vis, int32_t eig_mode, int32_t k_rule,
                       float delta, int32_t shrink, float *d_evals, float *d_evecs,
                       int32_t *d_counts, uint16_t *d_proj_f16, void *stream);
+
+/* The effective weights the last sf_covariance_eig in SAME_POL mode (or sf_run_adaptive) left in
+ * plan memory -- the pair sf_beamform applies -- copied into d_weff: float pairs [C][Pol][2B][R][2],
+ * slot 0 (rows 0..B-1) = W diag(d), slot 1 (rows B..2B-1) = (W P) diag(d).  The reference keeps the
+ * same pair in device memory only (weights_rfi_mitigated, slots 0 and 1,
+ * lambda_adaptive_beamformed_spectra_pipeline.hpp:764-790); this reads it out, e.g. to measure the
+ * null depth |w'a|^2 / |w a|^2 on a known interferer.  Asynchronous device-to-device copy. */
+int sf_get_effective_weights(sf_plan *plan, float *d_weff, void *stream);
 
 /* Beamform with the plan's effective weights: n_slots = 1 uses W diag(d),
  * n_slots = 2 uses the (original, projected) pair from sf_covariance_eig.
@@ -244,17 +274,23 @@ int sf_run_adaptive(sf_plan *plan, const int8_t *d_samples, const int16_t *d_sca
  * Takes the shape and caller-owned device buffers only (no plan):
  *   d_weights_f16  fp16 pairs [C][Pol][B][R][2]
  *   d_factors      float pairs [C][Pol][R][2] per-receiver gain x phasor, or NULL for 1
- *   d_delays       int32 [F] sub-packet delays in [-Tp, Tp], or NULL for 0
+ *   d_delays       int32 [F] sub-packet delays in [-Tp, Tp], or NULL for 0; a delay
+ *                  outside that range is replaced by 0 and raises SF_DEV_BAD_DELAY
+ *                  in the status word (the kernels never read outside the samples)
  *   d_fixed_counts int32 [C] K per channel for SF_K_FIXED, or NULL for 0
  *   d_counts       int32 [C][Pol] chosen K (may be NULL)
  *   d_beams_f16    fp16 [C][Pol][2B][T][2] (slot 0 original, slot 1 projected)
- *   d_status       uint32 device error bits the caller clears (may be NULL)
+ *   d_status       uint32 device error bits (sf_device_bits); the call only ORs bits
+ *                  in, so the caller clears it (may be NULL)
+ * Pointer alignment: samples 16 bytes, factors 8 bytes, weights and beams 4 bytes
+ * (else SF_ERR_INVALID_ARGUMENT).
  * Intermediates (visibilities, effective weights, ...) live in one 16 MiB
  * static device array per GPU, held from first use until the process exits;
  * shapes that need more (above about 530 channels of 36 receivers and 8 beams)
- * return SF_ERR_UNSUPPORTED.  The first call on a device resolves that
- * array's address (cudaGetSymbolAddress) and should come before any stream
- * capture.  Calls share the array and keep its last contents, so calls that
+ * return SF_ERR_UNSUPPORTED.  The first call on each device is the set-up
+ * call: it resolves the array's address (cudaGetSymbolAddress), which may load
+ * the library's device code and commit the 16 MiB, so make it outside the
+ * real-time path and before any stream capture; later calls allocate nothing.  Calls share the array and keep its last contents, so calls that
  * overlap on one GPU race: serialise them.  Allocates nothing (no cudaMalloc,
  * cudaFree or allocating library call). */
 int sf_run_adaptive_noalloc(const sf_shape *shape, const int8_t *d_samples,

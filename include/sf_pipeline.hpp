@@ -29,7 +29,8 @@
  * Config supplies the compile-time sizes the reference's LambdaConfig has:
  * NR_CHANNELS, NR_FPGA_SOURCES, NR_TIME_STEPS_PER_PACKET, NR_RECEIVERS,
  * NR_RECEIVERS_PER_PACKET, NR_POLARIZATIONS (2), NR_PACKETS_FOR_CORRELATION,
- * NR_BEAMS.
+ * NR_BEAMS, NR_CORRELATED_BLOCKS_TO_ACCUMULATE (and optionally
+ * FFT_DOWNSAMPLE_FACTOR); LambdaConfig itself serves.
  *
  * Behaviour as the reference: execute_pipeline copies the buffer's samples and
  * scales to the device, releases the ring buffer back to the state once the
@@ -50,20 +51,45 @@
  * (T not a power of two in [64, 16384]; Tp not 16, 32 or 64) skip the tail and
  * register no FFT block.
  *
- * Beam steering: set_beam_steering(SfBeamSteering<Config>) (sf_pointing.hpp)
- * registers every buffer's plan; execute_pipeline then calls maybe_refresh()
- * first, before any work of the run is enqueued, as the reference's pipelines
- * do with their BeamSteering (lambda_gpu_pipeline.hpp:454-456, 973).
+ * Constructors take the reference's arguments in the reference's order, so a
+ * host framework swaps only the class name:
+ *   SfLambdaCorrBeamOnlyGPUPipeline(num_buffers, h_weights, beam_steering,
+ *                                   nr_blocks_to_accumulate = Config::NR_CORRELATED_BLOCKS_TO_ACCUMULATE)
+ *       (lambda_corr_beam_only_gpu_pipeline.hpp:385-388)
+ *   SfLambdaGPUPipeline(num_buffers, h_weights, beam_steering,
+ *                       nr_blocks_to_accumulate = Config::NR_CORRELATED_BLOCKS_TO_ACCUMULATE)
+ *       (lambda_gpu_pipeline.hpp:784-786)
+ *   SfLambdaAdaptivePipeline(num_buffers, h_weights, nr_signal_eigenvectors, min_freq_channel,
+ *                            beam_steering, shrink_eigenvalues = false,
+ *                            detect_signal_eigenmodes = false, detection_threshold_delta = 3.0f,
+ *                            eigenmode_stats_interval_seconds = 10.0)
+ *       (lambda_adaptive_beamformed_spectra_pipeline.hpp:1014-1019)
+ *
+ * Beam steering: beam_steering is either the reference's BeamSteering<T>
+ * (anything with register_buffer(BeamWeights *device_weights, cudaStream_t)
+ * and maybe_refresh(), common.hpp:245-303) -- every buffer's plan weights are
+ * registered with it and its asynchronous copies land in them -- or this
+ * library's SfBeamSteering<Config> (sf_pointing.hpp), which synthesises the
+ * weights on the device.  Either is inert without targets.  execute_pipeline
+ * calls maybe_refresh() first, before any work of the run is enqueued, as the
+ * reference's pipelines do (lambda_gpu_pipeline.hpp:454-456, 973); neither
+ * form synchronises with the GPU.  set_beam_steering() attaches one later.
  */
 #ifndef SF_PIPELINE_HPP
 #define SF_PIPELINE_HPP
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <chrono>
 #include <complex>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
+#include <functional>
+#include <iostream>
 #include <limits>
+#include <mutex>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -135,6 +161,20 @@ struct FftDownsample<Cfg, std::void_t<decltype(Cfg::FFT_DOWNSAMPLE_FACTOR)>> {
 
 constexpr bool pow2_in(int n, int lo, int hi) { return n >= lo && n <= hi && (n & (n - 1)) == 0; }
 
+// Steering objects: this library's SfBeamSteering (register_plan) or the
+// reference's BeamSteering<T> (register_buffer on the device weights).
+template <typename S, typename = void> struct HasRegisterPlan : std::false_type {};
+template <typename S>
+struct HasRegisterPlan<S, std::void_t<decltype(std::declval<S &>().register_plan(
+                              static_cast<sf_plan *>(nullptr), static_cast<cudaStream_t>(nullptr)))>>
+    : std::true_type {};
+template <typename S, typename = void> struct HasRegisterBuffer : std::false_type {};
+template <typename S>
+struct HasRegisterBuffer<S, std::void_t<typename S::BeamWeights,
+                                        decltype(std::declval<S &>().register_buffer(
+                                            static_cast<typename S::BeamWeights *>(nullptr),
+                                            static_cast<cudaStream_t>(nullptr)))>> : std::true_type {};
+
 }  // namespace detail
 
 // Shared machinery of the three adapters.  Base is the host framework's
@@ -165,7 +205,7 @@ template <typename Config, typename Base, int Mode> class SfPipelineBase : publi
 
   // weights: the BeamWeightsT<Config> payload, std::complex<__half>[C][Pol][B][R]
   template <typename Weights>
-  SfPipelineBase(int num_buffers, const Weights *h_weights, int nr_blocks_to_accumulate)
+  SfPipelineBase(int num_buffers, Weights *h_weights, int nr_blocks_to_accumulate)
       : nr_blocks_(nr_blocks_to_accumulate > 0 ? nr_blocks_to_accumulate : 1) {
     static_assert(sizeof(Weights) == sizeof(uint16_t) * 2 * C * POL * B * R,
                   "weights must be [C][Pol][B][R] complex fp16");
@@ -251,16 +291,29 @@ template <typename Config, typename Base, int Mode> class SfPipelineBase : publi
       detail::check(sf_set_stream_permutation(b->plan, rp.data(), pp.data(), b->stream), "sf_set_stream_permutation");
   }
 
-  // Keep the beams pointed at the steering's targets (inert without targets).
-  void set_beam_steering(SfBeamSteering<Config> steering) {
-    steering_ = std::move(steering);
-    for (auto &b : buffers_) steering_.register_plan(b->plan, b->stream);
+  // Keep the beams pointed at the steering's targets (inert without targets):
+  // an SfBeamSteering<Config> or the reference's BeamSteering<T>.
+  template <typename Steering> void set_beam_steering(Steering steering) {
+    static_assert(detail::HasRegisterPlan<Steering>::value || detail::HasRegisterBuffer<Steering>::value,
+                  "beam_steering needs register_plan(sf_plan*, cudaStream_t) or "
+                  "register_buffer(BeamWeights*, cudaStream_t)");
+    auto held = std::make_shared<Steering>(std::move(steering));
+    for (auto &b : buffers_) {
+      if constexpr (detail::HasRegisterPlan<Steering>::value) {
+        held->register_plan(b->plan, b->stream);
+      } else {
+        void *dw = nullptr;
+        detail::check(sf_plan_weights_buffer(b->plan, &dw), "sf_plan_weights_buffer");
+        held->register_buffer(static_cast<typename Steering::BeamWeights *>(dw), b->stream);
+      }
+    }
+    refresh_steering_ = [held]() { held->maybe_refresh(); };
   }
 
   void execute_pipeline(FinalPacketData *packet_data, const bool dummy_run = false) override {
     if (!dummy_run && this->state_ == nullptr)
       throw std::logic_error("State has not been set on GPUPipeline object!");
-    steering_.maybe_refresh();
+    if (refresh_steering_) refresh_steering_();
     Buffer &b = *buffers_[current_];
     if (packet_data->get_samples_elements_size() != b.samples.bytes() ||
         packet_data->get_scales_element_size() != b.scales.bytes())
@@ -321,6 +374,14 @@ template <typename Config, typename Base, int Mode> class SfPipelineBase : publi
     vis_start_seq_ = std::numeric_limits<size_t>::max();
     vis_missing_ = 0;
     integrated_ = 0;
+  }
+
+  // Wait for every queued run and transfer, ignoring errors (destructors).
+  void synchronize_quietly() {
+    for (auto &b : buffers_) {
+      if (b->stream) cudaStreamSynchronize(b->stream);
+      if (b->host_stream) cudaStreamSynchronize(b->host_stream);
+    }
   }
 
   // Wait for every queued run and transfer (the reference's destructor syncs).
@@ -420,7 +481,7 @@ template <typename Config, typename Base, int Mode> class SfPipelineBase : publi
   }
 
   std::vector<std::unique_ptr<Buffer>> buffers_;
-  SfBeamSteering<Config> steering_;
+  std::function<void()> refresh_steering_;
   detail::DeviceArray<int64_t> accum_;
   detail::DeviceArray<float> vis_f32_;
   cudaEvent_t last_accumulate_ = nullptr;
@@ -437,10 +498,12 @@ class SfLambdaCorrBeamOnlyGPUPipeline : public SfPipelineBase<Config, Base, 0> {
   using Super = SfPipelineBase<Config, Base, 0>;
 
  public:
-  template <typename Weights>
-  SfLambdaCorrBeamOnlyGPUPipeline(int num_buffers, const Weights *h_weights,
-                                  int nr_blocks_to_accumulate = std::numeric_limits<int>::max())
-      : Super(num_buffers, h_weights, nr_blocks_to_accumulate) {}
+  template <typename Weights, typename Steering>
+  SfLambdaCorrBeamOnlyGPUPipeline(const int num_buffers, Weights *h_weights, Steering beam_steering,
+                                  int nr_blocks_to_accumulate = Config::NR_CORRELATED_BLOCKS_TO_ACCUMULATE)
+      : Super(num_buffers, h_weights, nr_blocks_to_accumulate) {
+    this->set_beam_steering(std::move(beam_steering));
+  }
 
  protected:
   void run_chain(typename Super::Buffer &b) override {
@@ -455,10 +518,12 @@ class SfLambdaGPUPipeline : public SfPipelineBase<Config, Base, 1> {
   using Super = SfPipelineBase<Config, Base, 1>;
 
  public:
-  template <typename Weights>
-  SfLambdaGPUPipeline(int num_buffers, const Weights *h_weights,
-                      int nr_blocks_to_accumulate = std::numeric_limits<int>::max())
-      : Super(num_buffers, h_weights, nr_blocks_to_accumulate) {}
+  template <typename Weights, typename Steering>
+  SfLambdaGPUPipeline(const int num_buffers, Weights *h_weights, Steering beam_steering,
+                      int nr_blocks_to_accumulate = Config::NR_CORRELATED_BLOCKS_TO_ACCUMULATE)
+      : Super(num_buffers, h_weights, nr_blocks_to_accumulate) {
+    this->set_beam_steering(std::move(beam_steering));
+  }
 
  protected:
   void run_chain(typename Super::Buffer &b) override {
@@ -472,21 +537,27 @@ class SfLambdaGPUPipeline : public SfPipelineBase<Config, Base, 1> {
 // whitened eigendecomposition, K (fixed map, detection or shrink), W P, and
 // 2B beams (original, projected).  nr_signal_eigenvectors maps absolute
 // frequency channel -> K (the reference's -e map); channels absent get 0.
+// Like the reference, visibilities are dumped only on an explicit
+// dump_visibilities() (the reference's is a no-op; this one lands the
+// integrated visibilities), and every run's nulled-mode counts are kept for
+// print_eigenmode_stats() (reference ..._pipeline.hpp:930-1000).
 template <typename Config, typename Base = GPUPipeline>
 class SfLambdaAdaptivePipeline : public SfPipelineBase<Config, Base, 2> {
   using Super = SfPipelineBase<Config, Base, 2>;
 
  public:
-  template <typename Weights>
-  SfLambdaAdaptivePipeline(int num_buffers, const Weights *h_weights,
-                           const std::unordered_map<int, int> &nr_signal_eigenvectors, int min_freq_channel,
-                           bool shrink_eigenvalues = false, bool detect_signal_eigenmodes = false,
-                           float detection_threshold_delta = 3.0f,
-                           int nr_blocks_to_accumulate = std::numeric_limits<int>::max())
-      : Super(num_buffers, h_weights, nr_blocks_to_accumulate),
+  template <typename Weights, typename Steering>
+  SfLambdaAdaptivePipeline(const int num_buffers, Weights *h_weights,
+                           const std::unordered_map<int, int> nr_signal_eigenvectors, const int min_freq_channel,
+                           Steering beam_steering, bool shrink_eigenvalues = false,
+                           bool detect_signal_eigenmodes = false, float detection_threshold_delta = 3.0f,
+                           double eigenmode_stats_interval_seconds = 10.0)
+      : Super(num_buffers, h_weights, std::numeric_limits<int>::max()),
         shrink_(shrink_eigenvalues),
         k_rule_(detect_signal_eigenmodes ? SF_K_DETECT : SF_K_FIXED),
-        delta_(detection_threshold_delta) {
+        delta_(detection_threshold_delta),
+        eigenmode_stats_interval_seconds_(eigenmode_stats_interval_seconds),
+        stats_(std::make_shared<Stats>()) {
     std::vector<int32_t> counts(Config::NR_CHANNELS, 0);
     for (int c = 0; c < Config::NR_CHANNELS; ++c) {
       const auto it = nr_signal_eigenvectors.find(min_freq_channel + c);
@@ -494,19 +565,90 @@ class SfLambdaAdaptivePipeline : public SfPipelineBase<Config, Base, 2> {
     }
     for (auto &b : this->buffers_)
       detail::check(sf_set_fixed_counts(b->plan, counts.data(), b->stream), "sf_set_fixed_counts");
+    staging_.resize(this->buffers_.size(), nullptr);
+    for (auto &h : staging_)
+      detail::check_cuda(cudaMallocHost(reinterpret_cast<void **>(&h), sizeof(int32_t) * Config::NR_CHANNELS * 2),
+                         "cudaMallocHost");
+    this->set_beam_steering(std::move(beam_steering));
+  }
+
+  ~SfLambdaAdaptivePipeline() {
+    this->synchronize_quietly();
+    for (auto h : staging_)
+      if (h) cudaFreeHost(h);
+  }
+
+  // The interval the host framework prints eigenmode statistics at (stored as
+  // the reference stores it; print_eigenmode_stats() does the printing).
+  double eigenmode_stats_interval_seconds() const { return eigenmode_stats_interval_seconds_; }
+
+  // Per (channel, pol): min / max / median / mean of the nulled-mode count over
+  // the runs since the last call, then the history is cleared.
+  void print_eigenmode_stats() {
+    std::vector<int32_t> samples;
+    {
+      std::lock_guard<std::mutex> lock(stats_->mu);
+      samples.swap(stats_->history);
+    }
+    const size_t per = static_cast<size_t>(Config::NR_CHANNELS) * 2;
+    if (samples.empty() || samples.size() % per != 0) return;
+    const size_t n = samples.size() / per;
+    std::cout << "Eigenmode nulling stats over last " << n << " samples" << std::endl;
+    for (int c = 0; c < Config::NR_CHANNELS; ++c)
+      for (int pol = 0; pol < 2; ++pol) {
+        std::vector<int32_t> series(n);
+        double sum = 0.0;
+        for (size_t i = 0; i < n; ++i) {
+          series[i] = samples[i * per + c * 2 + pol];
+          sum += series[i];
+        }
+        std::sort(series.begin(), series.end());
+        const double median = n % 2 == 0 ? 0.5 * (series[n / 2 - 1] + series[n / 2]) : series[n / 2];
+        std::cout << "  ch=" << c << " pol=" << pol << " min=" << series.front() << " max=" << series.back()
+                  << " median=" << median << " mean=" << sum / static_cast<double>(n) << std::endl;
+      }
+    std::fflush(stdout);
   }
 
  protected:
+  struct Stats {
+    std::mutex mu;
+    std::vector<int32_t> history;
+  };
+  struct StatsContext {
+    std::shared_ptr<Stats> stats;
+    const int32_t *counts;
+  };
+  static void record_counts_cb(void *data) {
+    auto *ctx = static_cast<StatsContext *>(data);
+    {
+      std::lock_guard<std::mutex> lock(ctx->stats->mu);
+      ctx->stats->history.insert(ctx->stats->history.end(), ctx->counts, ctx->counts + Config::NR_CHANNELS * 2);
+    }
+    delete ctx;
+  }
+
   void run_chain(typename Super::Buffer &b) override {
     detail::check(sf_run_adaptive(b.plan, b.samples.ptr, b.scales.ptr, k_rule_, delta_, shrink_ ? 1 : 0, b.vis.ptr,
                                   b.evals.ptr, nullptr, b.counts.ptr, b.beams.ptr, b.stream),
                   "sf_run_adaptive");
+    // the run's counts into the statistics history, off the GPU's path
+    size_t i = 0;
+    while (this->buffers_[i].get() != &b) ++i;
+    detail::check_cuda(cudaMemcpyAsync(staging_[i], b.counts.ptr, sizeof(int32_t) * Config::NR_CHANNELS * 2,
+                                       cudaMemcpyDeviceToHost, b.stream),
+                       "cudaMemcpyAsync");
+    auto *ctx = new StatsContext{stats_, staging_[i]};
+    detail::check_cuda(cudaLaunchHostFunc(b.stream, record_counts_cb, ctx), "cudaLaunchHostFunc");
   }
 
  private:
   bool shrink_;
   int32_t k_rule_;
   float delta_;
+  double eigenmode_stats_interval_seconds_;
+  std::shared_ptr<Stats> stats_;
+  std::vector<int32_t *> staging_;
 };
 
 }  // namespace sfgb

@@ -594,13 +594,15 @@ def adaptive_chain(shape, samples, scales, weights, k_fixed=None, detect=False,
 # Synthetic LAMBDA-shaped inputs (seeded)
 # --------------------------------------------------------------------------
 def synth_inputs(shape, seed=0, sigma=16.0, n_interferers=0, inr_db=20.0,
-                 frac_channels=0.1, scale_value=1):
+                 frac_channels=0.1, scale_value=1, return_steering=False):
     """Seeded synthetic integration in the packet layout.
 
     Noise: I, Q = clip(round(N(0, sigma^2)), -127, 127).  Interferers (in a
     random `frac_channels` of the channels) add sqrt(INR * 2 sigma^2) s(t) a
     with unit-norm random complex steering a and unit-power narrowband s(t);
     INR is the interferer eigenvalue over the per-receiver noise eigenvalue.
+    With return_steering, a fourth value maps each interfered channel to the
+    list of its interferers' steering vectors a [R][Pol] (unit norm per pol).
     """
     rng = np.random.Generator(np.random.PCG64(seed))
     C, R, T = shape.C, shape.R, shape.T
@@ -609,6 +611,7 @@ def synth_inputs(shape, seed=0, sigma=16.0, n_interferers=0, inr_db=20.0,
     re = rng.normal(0.0, sigma, size=(C, tt, R, NPOL))
     im = rng.normal(0.0, sigma, size=(C, tt, R, NPOL))
     rfi_ch = np.zeros(C, dtype=bool)
+    steering = {}
     if n_interferers > 0:
         nsel = max(1, int(round(frac_channels * C)))
         rfi_ch[rng.choice(C, size=nsel, replace=False)] = True
@@ -618,6 +621,7 @@ def synth_inputs(shape, seed=0, sigma=16.0, n_interferers=0, inr_db=20.0,
             for _ in range(n_interferers):
                 a = rng.normal(size=(R, NPOL)) + 1j * rng.normal(size=(R, NPOL))
                 a /= np.linalg.norm(a, axis=0, keepdims=True)
+                steering.setdefault(int(c), []).append(a.copy())
                 f0 = rng.uniform(-0.45, 0.45)
                 ph0 = rng.uniform(0, 2 * np.pi)
                 s = np.exp(1j * (2 * np.pi * f0 * t + ph0))
@@ -630,7 +634,27 @@ def synth_inputs(shape, seed=0, sigma=16.0, n_interferers=0, inr_db=20.0,
     x = np.stack([re, im], axis=-1).reshape(C, npk, shape.Tp, shape.F, shape.Rpp, NPOL, 2)
     samples = np.ascontiguousarray(np.transpose(x, (0, 1, 3, 2, 4, 5, 6)))
     scales = np.full(shape.scales_shape(), scale_value, dtype=np.int16)
+    if return_steering:
+        return samples, scales, rfi_ch, steering
     return samples, scales, rfi_ch
+
+
+def null_depth_db(w_eff, steering, n_beams):
+    """Null depth of the projected weights on known interferers: per
+    interfered channel, pol, beam and interferer, 10 log10(|w' a|^2 / |w a|^2)
+    with w = slot 0 (original) and w' = slot 1 (projected) of the effective
+    weights [C][Pol][2B][R] (complex) and a the interferer's steering vector.
+    The beam is sum_r w_r x_r (no conjugation), so the response is w . a."""
+    out = []
+    for c, vecs in steering.items():
+        for a in vecs:
+            for p in range(NPOL):
+                w0 = w_eff[c, p, :n_beams]
+                w1 = w_eff[c, p, n_beams:2 * n_beams]
+                r0 = np.abs(w0 @ a[:, p]) ** 2
+                r1 = np.abs(w1 @ a[:, p]) ** 2
+                out.append(10.0 * np.log10(np.maximum(r1, 1e-30) / np.maximum(r0, 1e-30)))
+    return np.concatenate(out) if out else np.zeros(0)
 
 
 def synth_weights(shape, seed=1, n_beams=None):

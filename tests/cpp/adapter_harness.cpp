@@ -7,10 +7,18 @@
 // (include/spatial/pipeline_base.hpp:9-40, packet_formats.hpp:50-66,
 // output.hpp:22-58, spatial.hpp:149-247).
 //
-// usage: adapter_harness <mode 0|1|2> <dir> [steer]
-//   steer: attach an SfBeamSteering (zenith targets; receiver r at antenna 200 + r,
-//          ENU (3 r, -2 r, 0.5 r + r % 3); receiver 4 a null input; 1.0 GHz + ch x 100 kHz
-//          from channel 50) before the first run
+// With -DSF_REFERENCE_PIPELINE_BASE the GPUPipeline base class comes from the
+// reference's own include/spatial/pipeline_base.hpp (self-contained; add
+// -I <reference>/include) instead of the restatement below.
+//
+// usage: adapter_harness <mode 0|1|2> <dir> [steer|refsteer]
+//   steer:    pass an SfBeamSteering (zenith targets; receiver r at antenna 200 + r,
+//             ENU (3 r, -2 r, 0.5 r + r % 3); receiver 4 a null input; 1.0 GHz + ch x 100 kHz
+//             from channel 50) as the constructor's beam_steering
+//   refsteer: pass a steering object with the reference BeamSteering<T>'s interface
+//             (register_buffer + maybe_refresh) whose first refresh copies
+//             dir/weights2.bin into every registered buffer's device weights
+//   otherwise an inert SfBeamSteering (no targets)
 //   reads  dir/samples.bin (int8, two integrations), dir/scales.bin (int16, two),
 //          dir/weights.bin (fp16 pairs)
 //   writes dir/beams_<run>.bin, dir/vis.bin (float, after one dump of both runs),
@@ -24,6 +32,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <limits>
 #include <memory>
 #include <mutex>
@@ -75,6 +84,9 @@ struct FinalPacketData {
   virtual int get_num_missing_packets() = 0;
 };
 
+#ifdef SF_REFERENCE_PIPELINE_BASE
+#include <spatial/pipeline_base.hpp>
+#else
 class GPUPipeline {
  public:
   virtual ~GPUPipeline() = default;
@@ -95,6 +107,7 @@ class GPUPipeline {
   int *subpacket_delays_ = nullptr;
   std::complex<float> *gains_ = nullptr;
 };
+#endif
 
 #include "sf_pipeline.hpp"
 
@@ -108,6 +121,7 @@ struct TestConfig {
   static constexpr int NR_POLARIZATIONS = 2;
   static constexpr int NR_PACKETS_FOR_CORRELATION = 8;
   static constexpr int NR_BEAMS = 3;
+  static constexpr int NR_CORRELATED_BLOCKS_TO_ACCUMULATE = 2;
   static constexpr int FFT_DOWNSAMPLE_FACTOR = 16;
 };
 using Cfg = TestConfig;
@@ -143,6 +157,24 @@ struct PinnedPacketData : FinalPacketData {
   bool *get_arrivals_ptr() override { return arrivals; }
   size_t get_arrivals_size() override { return kArrivals; }
   int get_num_missing_packets() override { return missing; }
+};
+
+// The reference BeamSteering<T>'s interface (common.hpp:245-303): buffers
+// register their device weights and stream; a due refresh enqueues one
+// asynchronous copy per buffer.  Here the first refresh is due at once and
+// copies a second weight set.
+struct ReferenceStyleSteering {
+  using BeamWeights = Weights;
+  std::shared_ptr<Weights> next;
+  std::vector<std::pair<BeamWeights *, cudaStream_t>> buffers;
+  bool done = false;
+  void register_buffer(BeamWeights *device_weights, cudaStream_t stream) { buffers.push_back({device_weights, stream}); }
+  bool maybe_refresh() {
+    if (done || !next) return false;
+    for (auto &b : buffers) cudaMemcpyAsync(b.first, next.get(), sizeof(BeamWeights), cudaMemcpyDefault, b.second);
+    done = true;
+    return true;
+  }
 };
 
 class RecordingState : public ProcessorStateBase {
@@ -246,9 +278,12 @@ int main(int argc, char **argv) {
         std::make_shared<HostOutput>(beam_bytes, vis_bytes, eval_bytes, evec_bytes, count_bytes, fft_bytes);
     RecordingState state;
 
-    std::unique_ptr<GPUPipeline> pipeline;
+    GPUPipeline *pipeline = nullptr;
+    std::function<void()> destroy;      // deletes through the concrete type
+    std::function<uint32_t()> status;   // device_status() of the concrete type
     int delays[Cfg::NR_FPGA_SOURCES] = {3, -5};
     const bool steer = argc > 3 && std::string(argv[3]) == "steer";
+    const bool refsteer = argc > 3 && std::string(argv[3]) == "refsteer";
     sfgb::SfBeamSteering<Cfg> steering;
     if (steer) {
       std::unordered_map<int, sfgb::ENUPosition> positions;
@@ -261,20 +296,32 @@ int main(int argc, char **argv) {
                                            sfgb::FrequencyPlan{1.0e9, 1.0e5}, 50,
                                            sfgb::ArrayLocation{52.9, 6.87, 30.0}, 1.0e6);
     }
+    ReferenceStyleSteering ref_steering;
+    if (refsteer) {
+      auto w2 = read_file(dir + "/weights2.bin", sizeof(Weights));
+      ref_steering.next = std::make_shared<Weights>();
+      std::memcpy(ref_steering.next.get(), w2.data(), sizeof(Weights));
+    }
+    // constructed exactly as the reference's pipelines are (argument order and defaults)
+    auto adopt = [&](auto *p) {
+      pipeline = p;
+      destroy = [p]() { delete p; };
+      status = [p]() { return p->device_status(); };
+    };
+    std::unordered_map<int, int> k_map;
+    for (int c = 0; c < C; ++c) k_map[100 + c] = c % 3;  // absolute channel -> K
     if (mode == 0) {
-      auto *p = new sfgb::SfLambdaCorrBeamOnlyGPUPipeline<Cfg>(2, weights.get(), 2);
-      if (steer) p->set_beam_steering(steering);
-      pipeline.reset(p);
+      if (refsteer) adopt(new sfgb::SfLambdaCorrBeamOnlyGPUPipeline<Cfg>(2, weights.get(), ref_steering));
+      else adopt(new sfgb::SfLambdaCorrBeamOnlyGPUPipeline<Cfg>(2, weights.get(), steering));
     } else if (mode == 1) {
-      auto *p = new sfgb::SfLambdaGPUPipeline<Cfg>(2, weights.get(), 2);
-      if (steer) p->set_beam_steering(steering);
-      pipeline.reset(p);
+      if (refsteer) adopt(new sfgb::SfLambdaGPUPipeline<Cfg>(2, weights.get(), ref_steering));
+      else adopt(new sfgb::SfLambdaGPUPipeline<Cfg>(2, weights.get(), steering));
     } else {
-      std::unordered_map<int, int> k_map;
-      for (int c = 0; c < C; ++c) k_map[100 + c] = c % 3;  // absolute channel -> K
-      auto *p = new sfgb::SfLambdaAdaptivePipeline<Cfg>(2, weights.get(), k_map, 100, false, false, 3.0f, 2);
-      if (steer) p->set_beam_steering(steering);
-      pipeline.reset(p);
+      if (refsteer)
+        adopt(new sfgb::SfLambdaAdaptivePipeline<Cfg>(2, weights.get(), k_map, 100, ref_steering, false, false, 3.0f,
+                                                      10.0));
+      else
+        adopt(new sfgb::SfLambdaAdaptivePipeline<Cfg>(2, weights.get(), k_map, 100, steering));
     }
     pipeline->set_state(&state);
     pipeline->set_output(output);
@@ -290,12 +337,11 @@ int main(int argc, char **argv) {
       packets[run].missing = run;
       pipeline->execute_pipeline(&packets[run]);  // the second run dumps the visibilities
     }
+    // the adaptive pipeline dumps only when asked (its reference counterpart's dump is a no-op)
+    if (mode == 2) pipeline->dump_visibilities(packets[1].end_seq_id);
     cudaDeviceSynchronize();
-    uint32_t bits = 0;
-    if (mode == 0) bits = static_cast<sfgb::SfLambdaCorrBeamOnlyGPUPipeline<Cfg> *>(pipeline.get())->device_status();
-    if (mode == 1) bits = static_cast<sfgb::SfLambdaGPUPipeline<Cfg> *>(pipeline.get())->device_status();
-    if (mode == 2) bits = static_cast<sfgb::SfLambdaAdaptivePipeline<Cfg> *>(pipeline.get())->device_status();
-    pipeline.reset();  // destructor waits for every stream
+    const uint32_t bits = status();
+    destroy();  // the destructor waits for every stream
 
     for (int run = 0; run < 2; ++run) {
       write_file(dir + "/beams_" + std::to_string(run) + ".bin", output->beams[run].data(), beam_bytes);

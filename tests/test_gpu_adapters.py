@@ -48,11 +48,13 @@ def inputs():
 
 
 def _run(harness, mode, inputs, tmp_path, steer=False):
+    """steer: False, True (an SfBeamSteering) or "refsteer" (reference-style steering)."""
     sh, samples, scales, w = inputs
     np.concatenate([s.reshape(-1) for s in samples]).astype(np.int8).tofile(tmp_path / "samples.bin")
     np.concatenate([s.reshape(-1) for s in scales]).astype(np.int16).tofile(tmp_path / "scales.bin")
     np.ascontiguousarray(w).tofile(tmp_path / "weights.bin")
-    cmd = [harness, str(mode), str(tmp_path)] + (["steer"] if steer else [])
+    flag = [] if not steer else (["refsteer"] if steer == "refsteer" else ["steer"])
+    cmd = [harness, str(mode), str(tmp_path)] + flag
     res = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
     assert res.returncode == 0, res.stderr
     proto = {}
@@ -198,3 +200,20 @@ def test_adapter_beam_steering(harness, inputs, tmp_path, mode):
         got = np.fromfile(tmp_path / f"beams_{run}.bin", dtype=np.float16).reshape(C, 2, slots * B, P * TP, 2)
         assert np.array_equal(got, ref["beams"][run])
         assert not np.array_equal(got, plain["beams"][run])
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2], ids=["corr_beam_only", "lambda_gpu", "adaptive"])
+def test_adapter_reference_style_steering(harness, inputs, tmp_path, mode):
+    """A steering object with the reference BeamSteering<T>'s interface
+    (register_buffer + maybe_refresh) passed as the constructor's third
+    argument: its asynchronous weight copies land in every buffer's plan, so
+    the landed beams equal a direct chain run with those weights."""
+    sh, samples, scales, w = inputs
+    w2 = orc.synth_weights(sh, seed=17).astype(np.float16)
+    np.ascontiguousarray(w2).tofile(tmp_path / "weights2.bin")
+    _run(harness, mode, inputs, tmp_path, steer="refsteer")
+    ref = _direct(mode, (sh, samples, scales, w2))
+    slots = 2 if mode == 2 else 1
+    for run in range(2):
+        got = np.fromfile(tmp_path / f"beams_{run}.bin", dtype=np.float16).reshape(C, 2, slots * B, P * TP, 2)
+        assert np.array_equal(got, ref["beams"][run])
