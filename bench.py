@@ -328,6 +328,7 @@ def run_ours(args, world, rank):
             "stages": stages}
     nulls = null_depth(plan, d_s[0], d_sc[0], vis, ev, cnt, beams, stream, sh, samples, scales, weights, tau,
                        steering)
+    uneven = run_uneven(args, dev, hbm) if (rank == 0 and not args.no_uneven) else None
     standin = library_standin(plan, d_s[0], d_sc[0], kernels["sf_eig_kernel"]["ms"], dev)
 
     line = {
@@ -346,11 +347,172 @@ def run_ours(args, world, rank):
                          for k, v in tail.items()},
         "e2e": e2e,
         "null_depth_db": nulls,
+        "uneven_batch": uneven,
         "library_standin": standin,
         "gpu_launches": 3 * args.steps,
         "clocks": clk,
     }
     return line
+
+
+UNEVEN = {"workload": "uneven_subarray_batch", "units": 8192, "antennas": [16, 36, 64, 128],
+          "antenna_mix": [0.4, 0.3, 0.2, 0.1], "polarizations": 2, "samples_per_integration": 4096, "beams": 8,
+          "beam_slots": 2, "interferers": "0-4 per unit", "inr_db": [5.0, 30.0], "k_rule": "lambda > 10 x median",
+          "launch": "CUDA graph: persistent correlator + eigensolver size classes + persistent beamformer"}
+
+
+def synth_uneven_on_device(bt, receivers, T, seed, dev):
+    """Seeded synthetic units of the uneven batch, made on the device (5.7 GB
+    of int8 would take minutes in numpy): noise clip(round(N(0, 16^2))) plus
+    0..4 narrowband interferers per unit at INR U[5, 30] dB."""
+    import torch
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    samples = torch.empty(bt.totals["samples"], dtype=torch.int8, device=dev)
+    recv = np.asarray(receivers)
+    t = torch.arange(T, device=dev, dtype=torch.float32)
+    for R in sorted(set(recv.tolist())):
+        units = np.flatnonzero(recv == R)
+        for c0 in range(0, len(units), 64):
+            us = units[c0:c0 + 64]
+            n = len(us)
+            x = torch.randn((n, T, R, 2, 2), generator=g, device=dev) * 16.0
+            n_int = torch.randint(0, 5, (n,), generator=g, device=dev)
+            for k in range(4):
+                inr = 10.0 ** (torch.rand(n, generator=g, device=dev) * 2.5 + 0.5)  # 5..30 dB
+                amp = torch.sqrt(inr * 2.0 * 16.0 ** 2) * (n_int > k).float()
+                a = torch.complex(torch.randn((n, R, 2), generator=g, device=dev),
+                                  torch.randn((n, R, 2), generator=g, device=dev))
+                a = a / torch.linalg.vector_norm(a, dim=1, keepdim=True)
+                f0 = torch.rand(n, generator=g, device=dev) * 0.9 - 0.45
+                ph = torch.rand(n, generator=g, device=dev) * 2 * np.pi
+                ang = 2 * np.pi * f0[:, None] * t[None] + ph[:, None]  # [n][T]
+                s_re = (amp[:, None] * torch.cos(ang))[:, :, None, None]
+                s_im = (amp[:, None] * torch.sin(ang))[:, :, None, None]
+                a_re, a_im = a.real[:, None], a.imag[:, None]  # [n][1][R][Pol]
+                x[..., 0] += s_re * a_re - s_im * a_im
+                x[..., 1] += s_re * a_im + s_im * a_re
+            x = torch.clamp(torch.round(x), -127, 127).to(torch.int8)
+            # units of one class are contiguous, in unit order
+            o = int(bt.layout["samples"][us[0]])
+            samples[o:o + x.numel()] = x.reshape(-1)
+            assert int(bt.layout["samples"][us[-1]]) == o + (n - 1) * T * R * 4
+    return samples
+
+
+def run_uneven(args, dev, hbm):
+    """The uneven-batching workload: 8192 channel-integrations of sub-arrays of
+    16/36/64/128 antennas (40/30/20/10 %), T = 4096, 8 beams x 2 slots, K from
+    the 10x-noise-floor rule; autotuned, then one CUDA-graph replay per step."""
+    import torch
+    import sfgb
+    import sf_oracle as orc
+    n_units, T, Bu = UNEVEN["units"], UNEVEN["samples_per_integration"], UNEVEN["beams"]
+    rng = np.random.default_rng(7)
+    recv = rng.choice(UNEVEN["antennas"], size=n_units, p=UNEVEN["antenna_mix"]).astype(np.int32)
+    bt = sfgb.Batch(recv, T, Bu)
+    ws = []
+    for R in recv:
+        ph = rng.uniform(0, 2 * np.pi, size=(2, Bu, int(R)))
+        ws.append(np.stack([np.cos(ph), np.sin(ph)], axis=-1).astype(np.float16))
+    bt.set_weights(bt.pack_weights(ws))
+    samples = synth_uneven_on_device(bt, recv, T, 11, dev)
+    stream = torch.cuda.Stream(device=dev)
+    vis = torch.empty(bt.totals["vis"], dtype=torch.int32, device=dev)
+    ev = torch.empty(bt.totals["evals"], dtype=torch.float32, device=dev)
+    cnt = torch.empty((n_units, 2), dtype=torch.int32, device=dev)
+    beams = torch.empty(2 * bt.totals["beams"], dtype=torch.float16, device=dev)
+    tuned = bt.autotune(samples, sfgb.SF_K_NOISE_FLOOR, 10.0, vis, ev, cnt, beams, stream=stream)
+
+    def step():
+        bt.run(samples, sfgb.SF_K_NOISE_FLOOR, 10.0, False, vis, ev, cnt, beams, stream=stream)
+
+    step()
+    stream.synchronize()
+    rc, bits = bt.status(stream)
+    if rc != 0:
+        raise RuntimeError(f"uneven batch: device status 0x{bits:x}")
+    # oracle gate on this very workload: two units of every size class
+    v, e, k, y = vis.cpu().numpy(), ev.cpu().numpy(), cnt.cpu().numpy(), beams.cpu().numpy()
+    checked = []
+    for R in UNEVEN["antennas"]:
+        for u in np.flatnonzero(recv == R)[:2]:
+            o = int(bt.layout["samples"][u])
+            x = samples[o:o + T * int(R) * 4].cpu().numpy().reshape(T, int(R), 2, 2)
+            ref = orc.unit_chain(x, ws[u], "fixed", k_fixed=k[u])
+            if not np.array_equal(bt.unit_vis(v, u), ref["vis"]):
+                raise RuntimeError(f"uneven batch: unit {u} visibilities differ from the oracle")
+            for p in range(2):
+                if k[u, p] != orc.noise_floor_k_f32(bt.unit_evals(e, u)[p], 10.0):
+                    raise RuntimeError(f"uneven batch: unit {u} K differs from the rule")
+            yb = bt.unit_beams(y, u).astype(np.float64)
+            err = np.abs(yb[..., 0] + 1j * yb[..., 1] - ref["beams"])
+            if not np.all(err <= 2.0 ** -8 * np.abs(ref["beams"]) + 0.05 +
+                          2e-3 * np.abs(ref["beams"]).max(axis=-1, keepdims=True)):
+                raise RuntimeError(f"uneven batch: unit {u} beams differ from the oracle")
+            checked.append(int(u))
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        step()
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            g.replay()
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = max(3, args.steps // 2)
+        e0.record(stream)
+        for _ in range(reps):
+            g.replay()
+        e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    rc, bits = bt.status(stream)
+    if rc != 0:
+        raise RuntimeError(f"uneven batch: device status 0x{bits:x} after timing")
+    # stage times (graph replays of each stage alone)
+    stages = {}
+    for name, fn in (("corr", lambda: bt.correlate(samples, vis, stream=stream)),
+                     ("eig", lambda: bt.covariance_eig(vis, sfgb.SF_K_NOISE_FLOOR, 10.0, False, ev, cnt,
+                                                       stream=stream)),
+                     ("beam", lambda: bt.beamform(samples, beams, stream=stream))):
+        gs = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(gs, stream=stream):
+            fn()
+        with torch.cuda.stream(stream):
+            gs.replay()
+            stream.synchronize()
+            e0.record(stream)
+            for _ in range(3):
+                gs.replay()
+            e1.record(stream)
+        e1.synchronize()
+        stages[name] = round(e0.elapsed_time(e1) / 3, 4)
+    r = recv.astype(np.int64)
+    samp_bytes = int((4 * r * T).sum())
+    vis_bytes = int((16 * r * (r + 1)).sum())
+    beam_bytes = n_units * 2 * 2 * Bu * T * 4
+    chain_bytes = samp_bytes + vis_bytes + n_units * 8 * Bu * 2 * T  # the per-unit convention of the chain
+    value = n_units / (ms / 1e3)
+    out = {"value": round(value, 1), "unit": UNIT, "ms_per_step": round(ms, 4), "config": UNEVEN,
+           "units_by_antennas": {str(R): int((recv == R).sum()) for R in UNEVEN["antennas"]},
+           "k_histogram": np.bincount(k.reshape(-1), minlength=5)[:8].tolist(),
+           "stages_ms": stages,
+           "roofline": {
+               "chain": {"bound": "hbm", "bytes_per_step": chain_bytes,
+                         "achieved": round(chain_bytes / (ms / 1e3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
+                         "frac": round(chain_bytes / (ms / 1e3) / 1e9 / hbm, 4)},
+               "corr": {"bound": "hbm", "bytes": samp_bytes + vis_bytes,
+                        "achieved": round((samp_bytes + vis_bytes) / (stages["corr"] / 1e3) / 1e9, 1),
+                        "frac": round((samp_bytes + vis_bytes) / (stages["corr"] / 1e3) / 1e9 / hbm, 4)},
+               "beam": {"bound": "hbm", "bytes": samp_bytes + beam_bytes,
+                        "achieved": round((samp_bytes + beam_bytes) / (stages["beam"] / 1e3) / 1e9, 1),
+                        "frac": round((samp_bytes + beam_bytes) / (stages["beam"] / 1e3) / 1e9 / hbm, 4)},
+               "eig": {"bound": "latency", "matrices": 2 * n_units,
+                       "matrices_per_s": round(2 * n_units / (stages["eig"] / 1e3))}},
+           "autotune": tuned.get("choice"), "autotune_ms": tuned.get("ms"),
+           "oracle_checked_units": checked, "gpu_launches_per_step": 5}
+    bt.close()
+    return out
 
 
 def stage_rooflines(kernels, hbm):
@@ -662,6 +824,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--ref-channels", type=int, default=384)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven sub-array batch workload")
     ap.add_argument("--channels", type=int, default=C,
                     help="channels per integration (default: the 384-channel workload)")
     ap.add_argument("--only-stage", choices=["corr", "eig", "beam", "packet_spectra", "beam_spectra"],

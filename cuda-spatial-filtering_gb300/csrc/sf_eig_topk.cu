@@ -30,10 +30,11 @@ namespace {
 
 constexpr int NT = 128;  // threads per matrix
 constexpr int NW = NT / 32;
-constexpr int MAX_N = 64;
+constexpr int MAX_N = 128;
 constexpr int GROUP = 8;  // inverse-iteration vectors solved at once (one lane of warp 0 each)
 constexpr int INV_ITERS = 3;
 constexpr int MAX_B = 16;  // beams per pol handled by the projection step
+constexpr int MAX_XK = 64;  // eigenvectors of T held at once (K is clamped to this; n <= 64 holds all)
 
 struct TopkArgs {
   const int32_t *vis;
@@ -47,13 +48,20 @@ struct TopkArgs {
   int C, R, B, NBL;
   int k_rule, shrink;
   float delta;
+  // Batched form (uneven sub-arrays): matrix blockIdx.x is items[first_item + blockIdx.x],
+  // with its own size and offsets into the arrays above; NULL for the plan's uniform layout.
+  const SfEigItem *items;
+  int first_item;
 };
+
+// rows of the eigenvector workspace X for an n x n matrix
+__host__ __device__ inline int topk_xk(int n) { return n < MAX_XK ? n : MAX_XK; }
 
 __host__ __device__ inline size_t topk_floats(int n, int B) {
   // float2: A (n x (n+1)), 2 v, p, tau, Z (NW x n), Wp (B x n), W0 (B x n), coef (NW x B)
-  // float:  X (n x n), LU workspace (5 GROUP x n), d, e, e2, lam, sd
+  // float:  X (xk x n), LU workspace (5 GROUP x n), d, e, e2, lam, sd
   const size_t f2 = (size_t)n * (n + 1) + 4 * (size_t)n + (size_t)NW * n + 2 * (size_t)B * n + (size_t)NW * B;
-  const size_t f = (size_t)n * n + 5 * (size_t)GROUP * n + 5 * (size_t)n;
+  const size_t f = (size_t)topk_xk(n) * n + 5 * (size_t)GROUP * n + 5 * (size_t)n;
   return ((2 * f2 + f) + 3) & ~(size_t)3;
 }
 
@@ -152,7 +160,9 @@ __device__ __forceinline__ void make_reflector(float2 *A, int ld, int n, int k, 
   }
 }
 
-__global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
+// NPL: matrix rows per lane in the register-resident steps (n <= 32 NPL).
+template <int NPL>
+__global__ void __launch_bounds__(NT, NPL <= 2 ? 6 : 1) sf_eig_topk_kernel(const TopkArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ float s_red[4 * NW];
   __shared__ float s_scal[8];
@@ -160,11 +170,42 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int lane = tid & 31;
-  const int n = a.R;
-  const int ld = n + 1;
   const int B = a.B;
-  const int bt = blockIdx.x;  // c * 2 + p
-  const int c = bt >> 1;
+  // this matrix: size, packed upper triangle (baseline (i,j) at entry baseline_of(i,j), each entry
+  // [Pol][Pol][2] int32), receiver factors, weights [B][n], outputs
+  int n, pol, fixedK;
+  const int32_t *visb;
+  const float2 *dp;
+  const __half2 *w;
+  float2 *we;
+  float *ev_out;
+  int32_t *cnt_out;
+  if (a.items) {
+    const SfEigItem it = a.items[a.first_item + blockIdx.x];
+    n = it.n;
+    pol = it.pol;
+    visb = a.vis + it.vis_off;
+    dp = a.factors ? a.factors + it.factor_off : nullptr;
+    w = a.weights + it.weight_off;
+    we = a.weff + it.weff_off;
+    ev_out = a.evals ? a.evals + it.eval_off : nullptr;
+    cnt_out = a.counts ? a.counts + it.count_idx : nullptr;
+    fixedK = a.fixed_counts ? a.fixed_counts[it.count_idx] : 0;
+  } else {
+    const int bt = blockIdx.x;  // c * 2 + p
+    const int c = bt >> 1;
+    n = a.R;
+    pol = bt & 1;
+    visb = a.vis + (size_t)c * a.NBL * 8;
+    dp = a.factors + (size_t)bt * n;
+    w = a.weights + (size_t)bt * B * n;
+    we = a.weff + (size_t)bt * 2 * B * n;
+    ev_out = a.evals ? a.evals + (size_t)bt * n : nullptr;
+    cnt_out = a.counts ? a.counts + bt : nullptr;
+    fixedK = a.fixed_counts ? a.fixed_counts[c] : 0;
+  }
+  const int ld = n + 1;
+  const int xk = topk_xk(n);
 
   float2 *A = reinterpret_cast<float2 *>(smem);  // n x ld
   float2 *vbuf = A + n * ld;                     // reflectors k (even / odd k)
@@ -175,7 +216,7 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
   float2 *W0 = Wp + B * n;                       // the original weights B x n
   float2 *coef = W0 + B * n;                     // NW x B projection coefficients
   float *X = reinterpret_cast<float *>(coef + NW * B);  // top-K vectors of T, K x n
-  float *U0 = X + n * n;                         // LU workspace, GROUP x n each
+  float *U0 = X + xk * n;                        // LU workspace, GROUP x n each
   float *U1 = U0 + GROUP * n;
   float *U2 = U1 + GROUP * n;
   float *ML = U2 + GROUP * n;
@@ -186,14 +227,14 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
   float *lam = e2 + n;
   float *sd = lam + n;
 
-  const float2 *dp = a.factors + (size_t)bt * n;
-  const int p = bt & 1;
+  const int p = pol;
+  auto factor = [&](int i) { return dp ? dp[i] : make_float2(1.0f, 0.0f); };
 
   // ---- 1. covariance (upper triangle, Hermitian completion), whitening ----
   for (int i = tid; i < n; i += NT) {
-    const int32_t *v = a.vis + ((((size_t)c * a.NBL + baseline_of(i, i)) * 2 + p) * 2 + p) * 2;
+    const int32_t *v = visb + (((size_t)baseline_of(i, i) * 2 + p) * 2 + p) * 2;
     float2 x = make_float2(static_cast<float>(v[0]), static_cast<float>(v[1]));
-    x = cmulc(cmul(dp[i], x), dp[i]);
+    x = cmulc(cmul(factor(i), x), factor(i));
     sd[i] = sqrtf(fmaxf(x.x, 1e-10f));
   }
   __syncthreads();
@@ -202,9 +243,9 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
   for (int e0 = tid; e0 < n * n; e0 += NT) {
     const int i = e0 / n, j = e0 - (e0 / n) * n;
     if (j > i) continue;
-    const int32_t *v = a.vis + ((((size_t)c * a.NBL + baseline_of(j, i)) * 2 + p) * 2 + p) * 2;
+    const int32_t *v = visb + (((size_t)baseline_of(j, i) * 2 + p) * 2 + p) * 2;
     float2 x = make_float2(static_cast<float>(v[0]), static_cast<float>(v[1]));
-    x = cmulc(cmul(dp[j], x), dp[i]);  // element (j, i) of the upper triangle
+    x = cmulc(cmul(factor(j), x), factor(i));  // element (j, i) of the upper triangle
     const float inv = 1.0f / (sd[i] * sd[j]);
     A[i * ld + j] = i == j ? make_float2(x.x * inv, 0.0f) : make_float2(x.x * inv, -x.y * inv);
     if (j < i) A[j * ld + i] = make_float2(x.x * inv, x.y * inv);
@@ -225,7 +266,9 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
     if (tau.x != 0.0f || tau.y != 0.0f) {
       // p = tau A22 v, A22 Hermitian held in both triangles: two threads per
       // row, even / odd columns
-      const int i = tid >> 1, h = tid & 1;
+      const int h = tid & 1;
+      float dre = 0.0f, dim = 0.0f;
+      for (int i = tid >> 1; i - (tid >> 1) < m; i += NT / 2) {  // uniform trip count per warp
       float2 acc0 = make_float2(0.0f, 0.0f), acc1 = make_float2(0.0f, 0.0f);
       if (i < m) {
         // four loads in flight before their products
@@ -258,13 +301,13 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
       float2 acc = make_float2(acc0.x + acc1.x, acc0.y + acc1.y);
       acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 1);
       acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 1);
-      float dre = 0.0f, dim = 0.0f;
       if (i < m && h == 0) {
         const float2 pi = cmul(tau, acc);
         pb[i] = pi;
         const float2 t = cmulc(vb[i], pi);  // conj(p_i) v_i
-        dre = t.x;
-        dim = t.y;
+        dre += t.x;
+        dim += t.y;
+      }
       }
       warp_sum2(dre, dim);
       if (lane == 0) {
@@ -285,10 +328,10 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
         // reflector k+1 formed from it at once (LAPACK zlarfg): alpha is row 1,
         // x the rows below
         const float2 v0 = vb[0], p0 = pb[0];
-        float2 col[2];
+        float2 col[NPL];
         float part = 0.0f;
 #pragma unroll
-        for (int t = 0; t < 2; ++t) {
+        for (int t = 0; t < NPL; ++t) {
           const int ii = lane + 32 * t;
           col[t] = make_float2(0.0f, 0.0f);
           if (ii < m) {
@@ -320,7 +363,7 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
           }
           float2 *vn = vbuf + ((k + 1) & 1) * n;
 #pragma unroll
-          for (int t = 0; t < 2; ++t) {
+          for (int t = 0; t < NPL; ++t) {
             const int ii = lane + 32 * t;
             if (ii >= 2 && ii < m) {
               const float2 v = nonzero ? cmul(col[t], sc) : col[t];
@@ -335,7 +378,7 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
           }
         } else {
 #pragma unroll
-          for (int t = 0; t < 2; ++t) {
+          for (int t = 0; t < NPL; ++t) {
             const int ii = lane + 32 * t;
             if (ii >= 2 && ii < m) A22[ii * ld] = col[t];
           }
@@ -373,9 +416,9 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
   __syncthreads();
   for (int i = tid; i < n; i += NT) e2[i] = e[i] * e[i];
   // K of the fixed rule is known before any eigenvalue
-  const bool need_all = a.k_rule != SF_K_FIXED || a.evals != nullptr || a.shrink;
+  const bool need_all = a.k_rule != SF_K_FIXED || ev_out != nullptr || a.shrink;
   int Kfix = 0;
-  if (!need_all) Kfix = max(0, min(n, a.fixed_counts ? a.fixed_counts[c] : 0));
+  if (!need_all) Kfix = max(0, min(xk, fixedK));
   __syncthreads();
 
   // ---- 3. eigenvalues (Gershgorin bracket) ----
@@ -454,8 +497,8 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
     }
   }
   __syncthreads();
-  if (a.evals)
-    for (int j = tid; j < n; j += NT) a.evals[(size_t)bt * n + j] = lam[j];
+  if (ev_out)
+    for (int j = tid; j < n; j += NT) ev_out[j] = lam[j];
 
   // ---- 4. K ----
   if (tid == 0) {
@@ -471,11 +514,15 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
       const float med = 0.5f * (lam[(n - 1) / 2] + lam[n / 2]);
       for (int i = 0; i < n; ++i) K += lam[i] > a.delta * med;
     } else {
-      K = a.fixed_counts ? a.fixed_counts[c] : 0;
+      K = fixedK;
     }
     K = max(0, min(n, K));
+    if (K > xk) {  // more modes than the eigenvector workspace holds: null the top xk
+      atomicOr(a.status, SF_DEVERR_BAD_SHAPE);
+      K = xk;
+    }
     s_K = K;
-    if (a.counts) a.counts[bt] = K;
+    if (cnt_out) *cnt_out = K;
   }
   __syncthreads();
   const int K = s_K;
@@ -593,7 +640,6 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
   }
 
   // ---- 6./7. back-transform (one warp per vector), projected weights ----
-  const __half2 *w = a.weights + (size_t)bt * B * n;
   for (int e0 = tid; e0 < B * n; e0 += NT) {
     const float2 x = __half22float2(w[e0]);
     Wp[e0] = x;
@@ -613,19 +659,28 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
       // (lane holds elements lane and lane + 32, n <= 64); reflector k's v is 1
       // at k + 1, A[j][k] below it, 0 above
       const float *x = X + r * n;
-      const int i0 = lane, i1 = lane + 32;
-      float2 z0 = make_float2(i0 < n ? x[i0] : 0.0f, 0.0f);
-      float2 z1 = make_float2(i1 < n ? x[i1] : 0.0f, 0.0f);
+      float2 zz[NPL];
+#pragma unroll
+      for (int t = 0; t < NPL; ++t) {
+        const int ii = lane + 32 * t;
+        zz[t] = make_float2(ii < n ? x[ii] : 0.0f, 0.0f);
+      }
       for (int k = n - 2; k >= 0; --k) {
         const float2 tau = taus[k];
-        const float2 v0 = i0 > k + 1 && i0 < n ? A[i0 * ld + k] : make_float2(i0 == k + 1 ? 1.0f : 0.0f, 0.0f);
-        const float2 v1 = i1 > k + 1 && i1 < n ? A[i1 * ld + k] : make_float2(i1 == k + 1 ? 1.0f : 0.0f, 0.0f);
-        float dre = v0.x * z0.x + v0.y * z0.y + v1.x * z1.x + v1.y * z1.y;  // conj(v) z
-        float dim = v0.x * z0.y - v0.y * z0.x + v1.x * z1.y - v1.y * z1.x;
+        float2 vv[NPL];
+        float dre = 0.0f, dim = 0.0f;  // conj(v) z
+#pragma unroll
+        for (int t = 0; t < NPL; ++t) {
+          const int ii = lane + 32 * t;
+          vv[t] = ii > k + 1 && ii < n ? A[ii * ld + k] : make_float2(ii == k + 1 ? 1.0f : 0.0f, 0.0f);
+          dre += vv[t].x * zz[t].x + vv[t].y * zz[t].y;
+          dim += vv[t].x * zz[t].y - vv[t].y * zz[t].x;
+        }
         warp_sum2(dre, dim);
         const float2 sc = cmul(tau, make_float2(dre, dim));
-        z0 = make_float2(z0.x - (sc.x * v0.x - sc.y * v0.y), z0.y - (sc.x * v0.y + sc.y * v0.x));
-        z1 = make_float2(z1.x - (sc.x * v1.x - sc.y * v1.y), z1.y - (sc.x * v1.y + sc.y * v1.x));
+#pragma unroll
+        for (int t = 0; t < NPL; ++t)
+          zz[t] = make_float2(zz[t].x - (sc.x * vv[t].x - sc.y * vv[t].y), zz[t].y - (sc.x * vv[t].y + sc.y * vv[t].x));
       }
       float wgt = 1.0f;
       if (a.shrink) {
@@ -633,16 +688,22 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
         wgt = 1.0f - (lk > 0.0f ? lam_bar / lk : 0.0f);
       } else {
         // un-whiten and normalise
-        const float s0 = i0 < n ? sd[i0] : 0.0f, s1 = i1 < n ? sd[i1] : 0.0f;
-        z0 = make_float2(z0.x * s0, z0.y * s0);
-        z1 = make_float2(z1.x * s1, z1.y * s1);
-        const float nrm2 = warp_sum(z0.x * z0.x + z0.y * z0.y + z1.x * z1.x + z1.y * z1.y);
+        float part = 0.0f;
+#pragma unroll
+        for (int t = 0; t < NPL; ++t) {
+          const int ii = lane + 32 * t;
+          const float si = ii < n ? sd[ii] : 0.0f;
+          zz[t] = make_float2(zz[t].x * si, zz[t].y * si);
+          part += zz[t].x * zz[t].x + zz[t].y * zz[t].y;
+        }
+        const float nrm2 = warp_sum(part);
         const float inv = nrm2 > 0.0f ? rsqrtf(nrm2) : 0.0f;
-        z0 = make_float2(z0.x * inv, z0.y * inv);
-        z1 = make_float2(z1.x * inv, z1.y * inv);
+#pragma unroll
+        for (int t = 0; t < NPL; ++t) zz[t] = make_float2(zz[t].x * inv, zz[t].y * inv);
       }
-      if (i0 < n) z[i0] = z0;
-      if (i1 < n) z[i1] = z1;
+#pragma unroll
+      for (int t = 0; t < NPL; ++t)
+        if (lane + 32 * t < n) z[lane + 32 * t] = zz[t];
       // c_m = wgt (W_m . z) against the original weights: all partial sums
       // first, then the reductions
       {
@@ -652,10 +713,13 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
           cre[mm] = 0.0f;
           cim[mm] = 0.0f;
           if (mm < B) {
-            const float2 wa = i0 < n ? W0[mm * n + i0] : make_float2(0.0f, 0.0f);
-            const float2 wb = i1 < n ? W0[mm * n + i1] : make_float2(0.0f, 0.0f);
-            cre[mm] = wa.x * z0.x - wa.y * z0.y + wb.x * z1.x - wb.y * z1.y;
-            cim[mm] = wa.x * z0.y + wa.y * z0.x + wb.x * z1.y + wb.y * z1.x;
+#pragma unroll
+            for (int t = 0; t < NPL; ++t) {
+              const int ii = lane + 32 * t;
+              const float2 wa = ii < n ? W0[mm * n + ii] : make_float2(0.0f, 0.0f);
+              cre[mm] += wa.x * zz[t].x - wa.y * zz[t].y;
+              cim[mm] += wa.x * zz[t].y + wa.y * zz[t].x;
+            }
           }
         }
 #pragma unroll
@@ -682,11 +746,10 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
     }
     __syncthreads();
   }
-  float2 *we = a.weff + (size_t)bt * 2 * B * n;
   for (int e0 = tid; e0 < B * n; e0 += NT) {
     const int col = e0 - (e0 / n) * n;
-    we[e0] = cmul(W0[e0], dp[col]);
-    we[B * n + e0] = cmul(Wp[e0], dp[col]);
+    we[e0] = cmul(W0[e0], factor(col));
+    we[B * n + e0] = cmul(Wp[e0], factor(col));
   }
 }
 
@@ -695,7 +758,52 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_topk_kernel(const TopkArgs a) {
 size_t sf_eig_topk_smem(int n, int B) { return topk_floats(n, B) * sizeof(float); }
 
 int sf_eig_topk_supported(const sf_plan *p) {
-  return p->R <= MAX_N && p->B <= MAX_B && sf_eig_topk_smem(p->R, p->B) <= 200 * 1024;
+  return p->R <= 64 && p->B <= MAX_B && sf_eig_topk_smem(p->R, p->B) <= 200 * 1024;
+}
+
+int sf_eig_topk_max_n() { return MAX_N; }
+int sf_eig_topk_max_b() { return MAX_B; }
+
+cudaError_t sf_launch_eig_topk_items(const SfEigItem *items, int first, int count, int n_max, int B,
+                                     const int32_t *vis, const float2 *factors, const __half2 *weights,
+                                     const int32_t *fixed_counts, int k_rule, float delta, int shrink, float *evals,
+                                     int32_t *counts, float2 *weff, uint32_t *status, cudaStream_t stream) {
+  if (count <= 0) return cudaSuccess;
+  if (n_max > MAX_N || B > MAX_B) return cudaErrorInvalidValue;
+  TopkArgs a;
+  a.vis = vis;
+  a.factors = factors;
+  a.weights = weights;
+  a.fixed_counts = fixed_counts;
+  a.evals = evals;
+  a.counts = counts;
+  a.weff = weff;
+  a.status = status;
+  a.C = 0;
+  a.R = n_max;
+  a.B = B;
+  a.NBL = 0;
+  a.k_rule = k_rule;
+  a.shrink = shrink;
+  a.delta = delta;
+  a.items = items;
+  a.first_item = first;
+  const size_t smem = sf_eig_topk_smem(n_max, B);
+  cudaError_t e;
+  if (n_max <= 32) {
+    e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<1>), smem);
+    if (e != cudaSuccess) return e;
+    sf_eig_topk_kernel<1><<<count, NT, smem, stream>>>(a);
+  } else if (n_max <= 64) {
+    e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<2>), smem);
+    if (e != cudaSuccess) return e;
+    sf_eig_topk_kernel<2><<<count, NT, smem, stream>>>(a);
+  } else {
+    e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<4>), smem);
+    if (e != cudaSuccess) return e;
+    sf_eig_topk_kernel<4><<<count, NT, smem, stream>>>(a);
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t sf_launch_eig_topk(const sf_plan *p, const int32_t *vis, int k_rule, float delta, int shrink,
@@ -716,9 +824,11 @@ cudaError_t sf_launch_eig_topk(const sf_plan *p, const int32_t *vis, int k_rule,
   a.k_rule = k_rule;
   a.shrink = shrink;
   a.delta = delta;
+  a.items = nullptr;
+  a.first_item = 0;
   const size_t smem = sf_eig_topk_smem(p->R, p->B);
-  cudaError_t e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel), smem);
+  cudaError_t e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<2>), smem);
   if (e != cudaSuccess) return e;
-  sf_eig_topk_kernel<<<p->C * 2, NT, smem, stream>>>(a);
+  sf_eig_topk_kernel<2><<<p->C * 2, NT, smem, stream>>>(a);
   return cudaGetLastError();
 }

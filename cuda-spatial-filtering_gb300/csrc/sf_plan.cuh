@@ -85,7 +85,23 @@ cudaError_t sf_launch_eig(const sf_plan *p, const int32_t *vis, int eig_mode, in
                           __half2 *proj, cudaStream_t stream);
 int sf_eig_supported(const sf_plan *p, char *why, size_t why_len);
 
+// One matrix of the batched (uneven sub-array) eigensolver: an n x n same-pol
+// covariance read from the packed int32 upper triangle at vis + vis_off
+// ([baseline][Pol][Pol][2]), receiver factors at factor_off ([n] float2, or
+// none), weights at weight_off ([B][n] half2), effective weights written at
+// weff_off ([2B][n] float2), eigenvalues at eval_off ([n]), K at count_idx.
+struct SfEigItem {
+  long long vis_off, factor_off, weight_off, weff_off, eval_off;
+  int n, pol, count_idx, unit;
+};
+
 size_t sf_eig_topk_smem(int n, int B);
+int sf_eig_topk_max_n();
+int sf_eig_topk_max_b();
+cudaError_t sf_launch_eig_topk_items(const SfEigItem *items, int first, int count, int n_max, int B,
+                                     const int32_t *vis, const float2 *factors, const __half2 *weights,
+                                     const int32_t *fixed_counts, int k_rule, float delta, int shrink, float *evals,
+                                     int32_t *counts, float2 *weff, uint32_t *status, cudaStream_t stream);
 int sf_eig_topk_supported(const sf_plan *p);
 cudaError_t sf_launch_eig_topk(const sf_plan *p, const int32_t *vis, int k_rule, float delta, int shrink,
                                float *evals, int32_t *counts, cudaStream_t stream);

@@ -82,6 +82,17 @@ _SIGS = {
     "sf_run_corr_beam": ([_P, _P, _P, _P, _P, _P], ctypes.c_int),
     "sf_run_lambda_gpu": ([_P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "sf_run_adaptive": ([_P, _P, _P, _I32, ctypes.c_float, _I32, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "sf_batch_create": ([_I32, _P, _I32, _I32, ctypes.POINTER(_P)], ctypes.c_int),
+    "sf_batch_destroy": ([_P], ctypes.c_int),
+    "sf_batch_get_layout": ([_P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "sf_batch_set_weights": ([_P, _P, _P], ctypes.c_int),
+    "sf_batch_set_fixed_counts": ([_P, _P, _P], ctypes.c_int),
+    "sf_batch_correlate": ([_P, _P, _P, _P], ctypes.c_int),
+    "sf_batch_covariance_eig": ([_P, _P, _I32, ctypes.c_float, _I32, _P, _P, _P], ctypes.c_int),
+    "sf_batch_beamform": ([_P, _P, _P, _P], ctypes.c_int),
+    "sf_batch_run": ([_P, _P, _I32, ctypes.c_float, _I32, _P, _P, _P, _P, _P], ctypes.c_int),
+    "sf_batch_status": ([_P, _P, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
+    "sf_batch_autotune": ([_P, _P, _I32, ctypes.c_float, _P, _P, _P, _P, _P, ctypes.c_char_p, _I32], ctypes.c_int),
     "sf_run_adaptive_noalloc": ([ctypes.POINTER(ShapeStruct), _P, _P, _P, _P, _P, _P, _I32, ctypes.c_float,
                                  _I32, _P, _P, _P, _P], ctypes.c_int),
 }
@@ -307,3 +318,110 @@ from .pipelines import (  # noqa: E402
 __all__ = ["Plan", "SfError", "lib", "header_symbols", "GPUPipeline", "LambdaGPUPipeline",
            "LambdaCorrBeamOnlyGPUPipeline", "LambdaAdaptiveBeamformedSpectraPipeline",
            "PacketData", "SingleHostMemoryOutput"]
+
+
+class Batch:
+    """A batch of sub-array units of uneven receiver counts (sf_batch_*).
+
+    ``receivers``: receiver count per unit; every unit has ``n_samples``
+    samples and ``n_beams`` beams.  ``layout`` holds the per-unit offsets of
+    every buffer (sample bytes, vis int32 elements, weight fp16 pairs, eval
+    floats, beam fp16 pairs) and ``totals`` the buffer sizes."""
+
+    def __init__(self, receivers, n_samples, n_beams):
+        import torch
+        if not torch.cuda.is_available():
+            raise RuntimeError("no CUDA device: the spatial-filtering kernels need an sm_103 GPU")
+        self.receivers = np.ascontiguousarray(receivers, dtype=np.int32)
+        self.n_units = int(self.receivers.size)
+        self.T, self.B = int(n_samples), int(n_beams)
+        h = ctypes.c_void_p()
+        _check(lib().sf_batch_create(self.n_units, self.receivers.ctypes.data_as(_P), self.T, self.B,
+                                     ctypes.byref(h)))
+        self._h = h
+        tot = np.zeros(5, np.int64)
+        offs = [np.zeros(self.n_units, np.int64) for _ in range(5)]
+        _check(lib().sf_batch_get_layout(self._h, tot.ctypes.data_as(_P), *[o.ctypes.data_as(_P) for o in offs]))
+        self.totals = {k: int(v) for k, v in zip(("samples", "vis", "weights", "evals", "beams"), tot)}
+        self.layout = dict(zip(("samples", "vis", "weights", "evals", "beams"), offs))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sf_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- host-side packing helpers (layout only; no arithmetic) ----
+    def pack_samples(self, units):
+        """List of int8 [T][R][Pol][2] -> one int8 array in the batch layout."""
+        out = np.zeros(self.totals["samples"], np.int8)
+        for u, x in enumerate(units):
+            o = int(self.layout["samples"][u])
+            out[o:o + x.size] = np.ascontiguousarray(x, np.int8).reshape(-1)
+        return out
+
+    def pack_weights(self, weights):
+        """List of fp16 [Pol][B][R][2] -> one fp16 array (pairs at the layout's offsets)."""
+        out = np.zeros(2 * self.totals["weights"], np.float16)
+        for u, w in enumerate(weights):
+            o = 2 * int(self.layout["weights"][u])
+            out[o:o + w.size] = np.ascontiguousarray(w, np.float16).reshape(-1)
+        return out
+
+    def unit_vis(self, vis, u):
+        R = int(self.receivers[u])
+        o = int(self.layout["vis"][u])
+        return vis[o:o + R * (R + 1) // 2 * 8].reshape(R * (R + 1) // 2, 2, 2, 2)
+
+    def unit_evals(self, evals, u):
+        R = int(self.receivers[u])
+        o = int(self.layout["evals"][u])
+        return evals[o:o + 2 * R].reshape(2, R)
+
+    def unit_beams(self, beams, u):
+        """fp16 [Pol][2B][T][2] of unit u from the flat beam buffer (fp16 elements)."""
+        o = 2 * int(self.layout["beams"][u])
+        n = 2 * 2 * self.B * self.T * 2
+        return beams[o:o + n].reshape(2, 2 * self.B, self.T, 2)
+
+    # ---- device calls ----
+    def set_weights(self, packed_f16, stream=None):
+        arr = np.ascontiguousarray(packed_f16, dtype=np.float16)
+        _check(lib().sf_batch_set_weights(self._h, arr.ctypes.data_as(_P), _stream(stream)))
+
+    def set_fixed_counts(self, counts=None, stream=None):
+        arr = None if counts is None else np.ascontiguousarray(counts, dtype=np.int32)
+        _check(lib().sf_batch_set_fixed_counts(self._h, None if arr is None else arr.ctypes.data_as(_P),
+                                               _stream(stream)))
+
+    def correlate(self, samples, vis, stream=None):
+        _check(lib().sf_batch_correlate(self._h, _ptr(samples), _ptr(vis), _stream(stream)))
+
+    def covariance_eig(self, vis, k_rule, delta, shrink, evals, counts, stream=None):
+        _check(lib().sf_batch_covariance_eig(self._h, _ptr(vis), int(k_rule), float(delta), int(bool(shrink)),
+                                             _ptr(evals), _ptr(counts), _stream(stream)))
+
+    def beamform(self, samples, beams, stream=None):
+        _check(lib().sf_batch_beamform(self._h, _ptr(samples), _ptr(beams), _stream(stream)))
+
+    def run(self, samples, k_rule, delta, shrink, vis, evals, counts, beams, stream=None):
+        _check(lib().sf_batch_run(self._h, _ptr(samples), int(k_rule), float(delta), int(bool(shrink)), _ptr(vis),
+                                  _ptr(evals), _ptr(counts), _ptr(beams), _stream(stream)))
+
+    def status(self, stream=None):
+        bits = ctypes.c_uint32(0)
+        rc = lib().sf_batch_status(self._h, _stream(stream), ctypes.byref(bits))
+        return rc, bits.value
+
+    def autotune(self, samples, k_rule, delta, vis, evals, counts, beams, stream=None):
+        """Runs the autotuner; returns its JSON record (dict)."""
+        import json
+        buf = ctypes.create_string_buffer(8192)
+        _check(lib().sf_batch_autotune(self._h, _ptr(samples), int(k_rule), float(delta), _ptr(vis), _ptr(evals),
+                                       _ptr(counts), _ptr(beams), _stream(stream), buf, len(buf)))
+        return json.loads(buf.value.decode())

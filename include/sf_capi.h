@@ -263,6 +263,53 @@ int sf_run_adaptive(sf_plan *plan, const int8_t *d_samples, const int16_t *d_sca
                     int32_t k_rule, float delta, int32_t shrink, int32_t *d_vis, float *d_evals,
                     float *d_evecs, int32_t *d_counts, uint16_t *d_beams_f16, void *stream);
 
+/* ---- batched sub-arrays of uneven size --------------------------------------- */
+
+/* A batch of units: one channel-integration each of a sub-array with its own receiver count
+ * (a multiple of 4, at most 128), all with n_samples (a multiple of 128) samples and n_beams beams.
+ * The whole mixed batch runs through one persistent tcgen05 correlator launch, the eigensolver
+ * (one launch per size class, side by side on forked streams) and one persistent tcgen05
+ * beamformer launch over a shared work list -- all capturable into one CUDA graph.  No counterpart
+ * in the reference, which compiles one receiver count per build (LambdaConfig template parameters,
+ * packet_formats.hpp:265-289) and replays one CUDA graph per buffer of that shape
+ * (lambda_gpu_pipeline.hpp:1005-1046); per unit the chain is the adaptive pipeline's
+ * (lambda_adaptive_beamformed_spectra_pipeline.hpp:563-798: corr -> whitened eig -> K ->
+ * I - U U^H -> W P -> 2B beams) with unit receiver factors.
+ *
+ * Layout (offsets per unit from sf_batch_get_layout; units are grouped by receiver count):
+ *   samples  int8  [T][R][Pol][2] at sample_off[u] bytes (the buffer 256-byte aligned)
+ *   vis      int32 [R(R+1)/2][Pol][Pol][2] at vis_off[u]        (packed upper triangle)
+ *   weights  fp16  [Pol][B][R][2] at weight_off[u] (fp16 pairs)
+ *   evals    float [Pol][R] at eval_off[u] (whitened, ascending);  counts int32 [u][Pol]
+ *   beams    fp16  [Pol][2B][T][2] at beam_off[u] (fp16 pairs; slot 0 original, slot 1 projected)
+ * totals[5] = {sample bytes, vis elements, weight pairs, eval elements, beam pairs}. */
+typedef struct sf_batch sf_batch;
+int sf_batch_create(int32_t n_units, const int32_t *h_receivers, int32_t n_samples, int32_t n_beams,
+                    sf_batch **out_batch);
+int sf_batch_destroy(sf_batch *batch);
+int sf_batch_get_layout(const sf_batch *batch, int64_t *totals, int64_t *sample_off, int64_t *vis_off,
+                        int64_t *weight_off, int64_t *eval_off, int64_t *beam_off);
+/* Host weights in the layout above (all units); synchronises `stream`. */
+int sf_batch_set_weights(sf_batch *batch, const uint16_t *h_weights_f16, void *stream);
+/* K per unit for SF_K_FIXED (both pols); NULL resets to 0; synchronises `stream`. */
+int sf_batch_set_fixed_counts(sf_batch *batch, const int32_t *h_counts, void *stream);
+int sf_batch_correlate(sf_batch *batch, const int8_t *d_samples, int32_t *d_vis, void *stream);
+int sf_batch_covariance_eig(sf_batch *batch, const int32_t *d_vis, int32_t k_rule, float delta, int32_t shrink,
+                            float *d_evals, int32_t *d_counts, void *stream);
+int sf_batch_beamform(sf_batch *batch, const int8_t *d_samples, uint16_t *d_beams_f16, void *stream);
+/* The three stages; every call only enqueues work on `stream` (capturable). */
+int sf_batch_run(sf_batch *batch, const int8_t *d_samples, int32_t k_rule, float delta, int32_t shrink,
+                 int32_t *d_vis, float *d_evals, int32_t *d_counts, uint16_t *d_beams_f16, void *stream);
+/* Reads and clears the batch's device error bits; synchronises `stream`. */
+int sf_batch_status(sf_batch *batch, void *stream, uint32_t *out_bits);
+/* Times candidate work-list packings, ring depths and eigensolver concurrency on the given buffers
+ * (CUDA events on `stream`, which it synchronises: call it at set-up, outside any capture), keeps
+ * the fastest for later calls and writes a JSON record of every candidate and the choice into
+ * `report` (if not NULL). */
+int sf_batch_autotune(sf_batch *batch, const int8_t *d_samples, int32_t k_rule, float delta, int32_t *d_vis,
+                      float *d_evals, int32_t *d_counts, uint16_t *d_beams_f16, void *stream, char *report,
+                      int32_t report_len);
+
 /* ---- allocation-free variant ------------------------------------------------ */
 
 /* The adaptive chain of sf_run_adaptive for callers that cannot allocate

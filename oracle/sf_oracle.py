@@ -665,3 +665,96 @@ def synth_weights(shape, seed=1, n_beams=None):
     ph = rng.uniform(0, 2 * np.pi, size=(shape.C, NPOL, B, shape.R))
     w = np.stack([np.cos(ph), np.sin(ph)], axis=-1).astype(np.float16)
     return w
+
+
+# --------------------------------------------------------------------------
+# Batched sub-arrays of uneven size: one unit = one channel-integration of a
+# sub-array, int8 samples [T][R][Pol][2] (no packet padding, unit scales),
+# through the adaptive chain with unit receiver factors.
+# --------------------------------------------------------------------------
+def unit_samples_split(x):
+    """int8 [T][R][Pol][2] -> re, im int64 [1][Pol][R][T] (the layout correlate() takes)."""
+    x = np.asarray(x).astype(np.int64)
+    re = np.transpose(x[..., 0], (2, 1, 0))[None]
+    im = np.transpose(x[..., 1], (2, 1, 0))[None]
+    return re, im
+
+
+def unit_chain(x, weights, k_rule="fixed", k_fixed=0, delta=10.0):
+    """The adaptive chain of one unit.  weights fp16 pairs [Pol][B][R][2].
+    k_rule: "fixed" (k_fixed, an int or a per-pol pair), "noise" (K =
+    #{lambda > delta x median}) or "detect" (detect_k_f32).  Returns vis (int64
+    [NBL][Pol][Pol][2]), evals [Pol][R] (whitened, LAPACK), counts [Pol],
+    w_eff [Pol][2B][R] and beams [Pol][2B][T] (complex)."""
+    T, R = x.shape[0], x.shape[1]
+    sh = Shape(1, 1, T, R, R, 1, 1)
+    re, im = unit_samples_split(x)
+    vis = correlate(sh, re, im)
+    vc = scaled_visibilities(sh, vis, receiver_factors(sh))
+    w = np.asarray(weights, np.float64)
+    wc = w[..., 0] + 1j * w[..., 1]  # [Pol][B][R]
+    B = wc.shape[1]
+    evals = np.zeros((NPOL, R))
+    counts = np.zeros(NPOL, np.int32)
+    w_eff = np.zeros((NPOL, 2 * B, R), np.complex128)
+    for p in range(NPOL):
+        m = unpack_hermitian(sh, vc, p, p)[0]
+        mw, s = whiten(m)
+        lam, v = eigh_ascending(mw)
+        if k_rule == "noise":
+            k = detect_k_noise_floor(lam, delta)
+        elif k_rule == "detect":
+            k = detect_k_f32(lam, delta)
+        else:
+            kf = np.atleast_1d(k_fixed)
+            k = int(kf[p] if kf.size > 1 else kf[0])
+        k = max(0, min(R, k))
+        u = unwhiten_normalize(v, s)
+        pm = null_projection(u, k)
+        evals[p] = lam
+        counts[p] = k
+        w_eff[p, :B] = wc[p]
+        w_eff[p, B:] = wc[p] @ pm
+    beams = np.einsum("pmr,prt->pmt", w_eff, re[0] + 1j * im[0])
+    return {"vis": vis[0], "evals": evals, "counts": counts, "w_eff": w_eff, "beams": beams}
+
+
+def synth_unit(R, T, rng, sigma=16.0, n_interferers=0, inr_db=(5.0, 30.0)):
+    """int8 [T][R][Pol][2]: noise clip(round(N(0, sigma^2))) plus n_interferers
+    narrowband interferers sqrt(INR 2 sigma^2) s(t) a, ||a|| = 1 per pol, INR
+    drawn uniformly in dB from inr_db."""
+    re = rng.normal(0.0, sigma, size=(T, R, NPOL))
+    im = rng.normal(0.0, sigma, size=(T, R, NPOL))
+    t = np.arange(T)
+    for _ in range(n_interferers):
+        inr = 10.0 ** (rng.uniform(*inr_db) / 10.0)
+        a = rng.normal(size=(R, NPOL)) + 1j * rng.normal(size=(R, NPOL))
+        a /= np.linalg.norm(a, axis=0, keepdims=True)
+        s = np.exp(1j * (2 * np.pi * rng.uniform(-0.45, 0.45) * t + rng.uniform(0, 2 * np.pi)))
+        sig = np.sqrt(inr * 2.0 * sigma ** 2) * s[:, None, None] * a[None]
+        re += np.real(sig)
+        im += np.imag(sig)
+    x = np.stack([np.clip(np.round(re), -127, 127), np.clip(np.round(im), -127, 127)], axis=-1)
+    return x.astype(np.int8)
+
+
+def synth_batch(receivers, T, B, seed=0, max_interferers=4):
+    """Units of the given receiver counts with 0..max_interferers interferers
+    each (INR uniform in [5, 30] dB) and unit-modulus random-phase weights
+    [Pol][B][R][2] fp16."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    xs, ws = [], []
+    for R in receivers:
+        xs.append(synth_unit(int(R), T, rng, n_interferers=int(rng.integers(0, max_interferers + 1))))
+        ph = rng.uniform(0, 2 * np.pi, size=(NPOL, B, int(R)))
+        ws.append(np.stack([np.cos(ph), np.sin(ph)], axis=-1).astype(np.float16))
+    return xs, ws
+
+
+def noise_floor_k_f32(evals, delta):
+    """The device's noise-floor rule in float32: K = #{lambda > delta x median},
+    median = (lambda[(n-1)/2] + lambda[n/2]) / 2 of the ascending eigenvalues."""
+    e = np.asarray(evals, dtype=np.float32)
+    n = e.size
+    med = np.float32(0.5) * (e[(n - 1) // 2] + e[n // 2])
+    return int(np.count_nonzero(e > np.float32(delta) * med))
