@@ -243,6 +243,13 @@ int sf_batch_create(int32_t n_units, const int32_t *h_receivers, int32_t n_sampl
     lo = limits[g];
   }
   b->eig_first[N_EIG_GROUPS] = (int)b->eig_items.size();
+  for (int g = 0; g < N_EIG_GROUPS; ++g)
+    if (b->eig_nmax[g] > 0 && sf_eig_topk_items_smem(b->eig_nmax[g], n_beams) > (size_t)sf_device_max_smem()) {
+      const int nm = b->eig_nmax[g];
+      free_batch(b);
+      return fail(SF_ERR_UNSUPPORTED, "%d receivers with %d beams exceed the eigensolver's shared memory", nm,
+                  n_beams);
+    }
   b->L.corr_grid = sms;
   b->L.beam_grid = sms;
   b->L.corr_ni = 2;

@@ -28,8 +28,7 @@
 
 namespace {
 
-constexpr int NT = 128;  // threads per matrix
-constexpr int NW = NT / 32;
+constexpr int NT_PLAN = 128;  // threads per matrix on the plan path (six CTAs per SM)
 constexpr int MAX_N = 128;
 constexpr int GROUP = 8;  // inverse-iteration vectors solved at once (one lane of warp 0 each)
 constexpr int INV_ITERS = 3;
@@ -52,12 +51,16 @@ struct TopkArgs {
   // with its own size and offsets into the arrays above; NULL for the plan's uniform layout.
   const SfEigItem *items;
   int first_item;
+  // Fallback form: the plan-layout matrices list[0 .. *list_count) (device-side count),
+  // walked grid-stride; NULL otherwise.
+  const int32_t *list;
+  const int32_t *list_count;
 };
 
 // rows of the eigenvector workspace X for an n x n matrix
 __host__ __device__ inline int topk_xk(int n) { return n < MAX_XK ? n : MAX_XK; }
 
-__host__ __device__ inline size_t topk_floats(int n, int B) {
+__host__ __device__ inline size_t topk_floats(int n, int B, int NW) {
   // float2: A (n x (n+1)), 2 v, p, tau, Z (NW x n), Wp (B x n), W0 (B x n), coef (NW x B)
   // float:  X (xk x n), LU workspace (5 GROUP x n), d, e, e2, lam, sd
   const size_t f2 = (size_t)n * (n + 1) + 4 * (size_t)n + (size_t)NW * n + 2 * (size_t)B * n + (size_t)NW * B;
@@ -160,9 +163,12 @@ __device__ __forceinline__ void make_reflector(float2 *A, int ld, int n, int k, 
   }
 }
 
-// NPL: matrix rows per lane in the register-resident steps (n <= 32 NPL).
-template <int NPL>
-__global__ void __launch_bounds__(NT, NPL <= 2 ? 6 : 1) sf_eig_topk_kernel(const TopkArgs a) {
+// NPL: matrix rows per lane in the register-resident steps (n <= 32 NPL);
+// NTT: threads per matrix.
+template <int NPL, int NTT>
+__global__ void __launch_bounds__(NTT, NTT <= 128 ? (NPL <= 2 ? 6 : 1) : 1) sf_eig_topk_kernel(const TopkArgs a) {
+  constexpr int NT = NTT;
+  constexpr int NW = NTT / 32;
   extern __shared__ __align__(16) uint8_t smem[];
   __shared__ float s_red[4 * NW];
   __shared__ float s_scal[8];
@@ -171,6 +177,9 @@ __global__ void __launch_bounds__(NT, NPL <= 2 ? 6 : 1) sf_eig_topk_kernel(const
   const int warp = tid >> 5;
   const int lane = tid & 31;
   const int B = a.B;
+  const int count = a.list ? *a.list_count : static_cast<int>(gridDim.x);
+  for (int mi = blockIdx.x; mi < count; mi += gridDim.x) {
+  if (mi != static_cast<int>(blockIdx.x)) __syncthreads();  // the previous matrix's shared memory is free
   // this matrix: size, packed upper triangle (baseline (i,j) at entry baseline_of(i,j), each entry
   // [Pol][Pol][2] int32), receiver factors, weights [B][n], outputs
   int n, pol, fixedK;
@@ -181,7 +190,7 @@ __global__ void __launch_bounds__(NT, NPL <= 2 ? 6 : 1) sf_eig_topk_kernel(const
   float *ev_out;
   int32_t *cnt_out;
   if (a.items) {
-    const SfEigItem it = a.items[a.first_item + blockIdx.x];
+    const SfEigItem it = a.items[a.first_item + mi];
     n = it.n;
     pol = it.pol;
     visb = a.vis + it.vis_off;
@@ -192,7 +201,7 @@ __global__ void __launch_bounds__(NT, NPL <= 2 ? 6 : 1) sf_eig_topk_kernel(const
     cnt_out = a.counts ? a.counts + it.count_idx : nullptr;
     fixedK = a.fixed_counts ? a.fixed_counts[it.count_idx] : 0;
   } else {
-    const int bt = blockIdx.x;  // c * 2 + p
+    const int bt = a.list ? a.list[mi] : mi;  // c * 2 + p
     const int c = bt >> 1;
     n = a.R;
     pol = bt & 1;
@@ -751,17 +760,25 @@ __global__ void __launch_bounds__(NT, NPL <= 2 ? 6 : 1) sf_eig_topk_kernel(const
     we[e0] = cmul(W0[e0], factor(col));
     we[B * n + e0] = cmul(Wp[e0], factor(col));
   }
+  }  // matrices of this CTA
 }
 
 }  // namespace
 
-size_t sf_eig_topk_smem(int n, int B) { return topk_floats(n, B) * sizeof(float); }
+size_t sf_eig_topk_smem(int n, int B) { return topk_floats(n, B, NT_PLAN / 32) * sizeof(float); }
 
 int sf_eig_topk_supported(const sf_plan *p) {
   return p->R <= 64 && p->B <= MAX_B && sf_eig_topk_smem(p->R, p->B) <= 200 * 1024;
 }
 
 int sf_eig_topk_max_n() { return MAX_N; }
+
+// Shared memory of one matrix of at most n_max receivers in the batched form
+// (the launch picks 128 / 256 / 512 threads for n_max <= 32 / 64 / 128).
+size_t sf_eig_topk_items_smem(int n_max, int B) {
+  const int nw = n_max <= 32 ? 4 : (n_max <= 64 ? 8 : 16);
+  return topk_floats(n_max, B, nw) * sizeof(float);
+}
 int sf_eig_topk_max_b() { return MAX_B; }
 
 cudaError_t sf_launch_eig_topk_items(const SfEigItem *items, int first, int count, int n_max, int B,
@@ -788,20 +805,25 @@ cudaError_t sf_launch_eig_topk_items(const SfEigItem *items, int first, int coun
   a.delta = delta;
   a.items = items;
   a.first_item = first;
-  const size_t smem = sf_eig_topk_smem(n_max, B);
+  a.list = nullptr;
+  a.list_count = nullptr;
+  // large matrices take more threads: the rank-2 update is spread over all warps but one
   cudaError_t e;
   if (n_max <= 32) {
-    e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<1>), smem);
+    const size_t smem = topk_floats(n_max, B, 4) * sizeof(float);
+    e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<1, 128>), smem);
     if (e != cudaSuccess) return e;
-    sf_eig_topk_kernel<1><<<count, NT, smem, stream>>>(a);
+    sf_eig_topk_kernel<1, 128><<<count, 128, smem, stream>>>(a);
   } else if (n_max <= 64) {
-    e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<2>), smem);
+    const size_t smem = topk_floats(n_max, B, 8) * sizeof(float);
+    e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<2, 256>), smem);
     if (e != cudaSuccess) return e;
-    sf_eig_topk_kernel<2><<<count, NT, smem, stream>>>(a);
+    sf_eig_topk_kernel<2, 256><<<count, 256, smem, stream>>>(a);
   } else {
-    e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<4>), smem);
+    const size_t smem = topk_floats(n_max, B, 16) * sizeof(float);
+    e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<4, 512>), smem);
     if (e != cudaSuccess) return e;
-    sf_eig_topk_kernel<4><<<count, NT, smem, stream>>>(a);
+    sf_eig_topk_kernel<4, 512><<<count, 512, smem, stream>>>(a);
   }
   return cudaGetLastError();
 }
@@ -826,9 +848,43 @@ cudaError_t sf_launch_eig_topk(const sf_plan *p, const int32_t *vis, int k_rule,
   a.delta = delta;
   a.items = nullptr;
   a.first_item = 0;
+  a.list = nullptr;
+  a.list_count = nullptr;
   const size_t smem = sf_eig_topk_smem(p->R, p->B);
-  cudaError_t e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<2>), smem);
+  cudaError_t e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<2, NT_PLAN>), smem);
   if (e != cudaSuccess) return e;
-  sf_eig_topk_kernel<2><<<p->C * 2, NT, smem, stream>>>(a);
+  sf_eig_topk_kernel<2, NT_PLAN><<<p->C * 2, NT_PLAN, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t sf_launch_eig_topk_list(const sf_plan *p, const int32_t *vis, const int32_t *list, const int32_t *list_count,
+                                    int max_count, int k_rule, float delta, int shrink, float *evals, int32_t *counts,
+                                    cudaStream_t stream) {
+  if (max_count <= 0) return cudaSuccess;
+  TopkArgs a;
+  a.vis = vis;
+  a.factors = p->d_factors;
+  a.weights = p->d_weights;
+  a.fixed_counts = p->d_fixed_counts;
+  a.evals = evals;
+  a.counts = counts;
+  a.weff = p->d_weff;
+  a.status = p->d_status;
+  a.C = p->C;
+  a.R = p->R;
+  a.B = p->B;
+  a.NBL = p->NBL;
+  a.k_rule = k_rule;
+  a.shrink = shrink;
+  a.delta = delta;
+  a.items = nullptr;
+  a.first_item = 0;
+  a.list = list;
+  a.list_count = list_count;
+  const size_t smem = sf_eig_topk_smem(p->R, p->B);
+  cudaError_t e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<2, NT_PLAN>), smem);
+  if (e != cudaSuccess) return e;
+  const int grid = max_count < 6 * p->num_sms ? max_count : 6 * p->num_sms;
+  sf_eig_topk_kernel<2, NT_PLAN><<<grid, NT_PLAN, smem, stream>>>(a);
   return cudaGetLastError();
 }

@@ -97,7 +97,12 @@ struct SfEigItem {
 
 size_t sf_eig_topk_smem(int n, int B);
 int sf_eig_topk_max_n();
+size_t sf_eig_topk_items_smem(int n_max, int B);
 int sf_eig_topk_max_b();
+// The plan-layout matrices list[0 .. *list_count) (count read on the device, at most max_count).
+cudaError_t sf_launch_eig_topk_list(const sf_plan *p, const int32_t *vis, const int32_t *list, const int32_t *list_count,
+                                    int max_count, int k_rule, float delta, int shrink, float *evals, int32_t *counts,
+                                    cudaStream_t stream);
 cudaError_t sf_launch_eig_topk_items(const SfEigItem *items, int first, int count, int n_max, int B,
                                      const int32_t *vis, const float2 *factors, const __half2 *weights,
                                      const int32_t *fixed_counts, int k_rule, float delta, int shrink, float *evals,

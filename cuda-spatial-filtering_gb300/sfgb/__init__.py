@@ -93,6 +93,22 @@ _SIGS = {
     "sf_batch_run": ([_P, _P, _I32, ctypes.c_float, _I32, _P, _P, _P, _P, _P], ctypes.c_int),
     "sf_batch_status": ([_P, _P, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
     "sf_batch_autotune": ([_P, _P, _I32, ctypes.c_float, _P, _P, _P, _P, _P, ctypes.c_char_p, _I32], ctypes.c_int),
+    "sf_proposer_create": ([_I32, _I32, _I32, ctypes.POINTER(_P)], ctypes.c_int),
+    "sf_proposer_destroy": ([_P], ctypes.c_int),
+    "sf_proposer_dims": ([_P, _P], ctypes.c_int),
+    "sf_proposer_set_params": ([_P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "sf_proposer_get_params": ([_P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "sf_proposer_features": ([_P, _P, _P, _I32, _P], ctypes.c_int),
+    "sf_proposer_targets": ([_P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "sf_proposer_infer": ([_P, _P, _I32, _P, _P], ctypes.c_int),
+    "sf_proposer_train_step": ([_P, _P, _P, _P, _I32, ctypes.c_float, _P, _P], ctypes.c_int),
+    "sf_proposer_status": ([_P, _P, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
+    "sf_covariance_eig_learned": ([_P, _P, _P, _I32, ctypes.c_float, _I32, ctypes.c_float, _P, _P, _P, _P],
+                                  ctypes.c_int),
+    "sf_run_adaptive_learned": ([_P, _P, _P, _P, _I32, ctypes.c_float, _I32, ctypes.c_float, _P, _P, _P, _P, _P],
+                                ctypes.c_int),
+    "sf_gemm_bf16": ([_I32, _I32, _I32, _P, _I32, _I32, _P, _I32, _I32, _I32, _P, _P, _I32, _P, _I32, _I32, _P, _P],
+                     ctypes.c_int),
     "sf_run_adaptive_noalloc": ([ctypes.POINTER(ShapeStruct), _P, _P, _P, _P, _P, _P, _I32, ctypes.c_float,
                                  _I32, _P, _P, _P, _P], ctypes.c_int),
 }
@@ -304,6 +320,25 @@ class Plan:
         _check(lib().sf_run_lambda_gpu(self._h, _ptr(samples), _ptr(scales), _ptr(vis), _ptr(evals),
                                        _ptr(evecs), _ptr(beams), _stream(stream)))
 
+    def proposer_features(self, vis, x, ld, stream=None):
+        _check(lib().sf_proposer_features(self._h, _ptr(vis), _ptr(x), int(ld), _stream(stream)))
+
+    def proposer_targets(self, vis, evals, evecs, targets, weights, stream=None):
+        _check(lib().sf_proposer_targets(self._h, _ptr(vis), _ptr(evals), _ptr(evecs), _ptr(targets), _ptr(weights),
+                                         _stream(stream)))
+
+    def covariance_eig_learned(self, proposer, vis, k_rule, delta, n_iter, tol, counts=None, ritz=None,
+                               fallback_count=None, stream=None):
+        _check(lib().sf_covariance_eig_learned(self._h, proposer._h, _ptr(vis), int(k_rule), float(delta), int(n_iter),
+                                               float(tol), _ptr(counts), _ptr(ritz), _ptr(fallback_count),
+                                               _stream(stream)))
+
+    def run_adaptive_learned(self, proposer, samples, scales, k_rule, delta, n_iter, tol, vis, counts, beams,
+                             fallback_count=None, stream=None):
+        _check(lib().sf_run_adaptive_learned(self._h, proposer._h, _ptr(samples), _ptr(scales), int(k_rule),
+                                             float(delta), int(n_iter), float(tol), _ptr(vis), _ptr(counts),
+                                             _ptr(beams), _ptr(fallback_count), _stream(stream)))
+
     def run_adaptive(self, samples, scales, k_rule, delta, shrink, vis, evals, evecs, counts, beams,
                      stream=None):
         _check(lib().sf_run_adaptive(self._h, _ptr(samples), _ptr(scales), int(k_rule), float(delta),
@@ -425,3 +460,14 @@ class Batch:
         _check(lib().sf_batch_autotune(self._h, _ptr(samples), int(k_rule), float(delta), _ptr(vis), _ptr(evals),
                                        _ptr(counts), _ptr(beams), _stream(stream), buf, len(buf)))
         return json.loads(buf.value.decode())
+
+
+def gemm_bf16(M, N, K, A, lda, a_mn, B, ldb, b_mn, epilogue, out, ldo, bias=None, mask=None, ldm=0, k_splits=1,
+              status=None, stream=None):
+    """sf_gemm_bf16 on device tensors (A, B, mask bf16; out bf16 or fp32)."""
+    import torch
+    st = status if status is not None else torch.zeros(1, dtype=torch.int32, device=A.device)
+    _check(lib().sf_gemm_bf16(int(M), int(N), int(K), _ptr(A), int(lda), int(a_mn), _ptr(B), int(ldb), int(b_mn),
+                              int(epilogue), _ptr(bias), _ptr(mask), int(ldm), _ptr(out), int(ldo), int(k_splits),
+                              _ptr(st), _stream(stream)))
+    return st
