@@ -329,6 +329,8 @@ def run_ours(args, world, rank):
     nulls = null_depth(plan, d_s[0], d_sc[0], vis, ev, cnt, beams, stream, sh, samples, scales, weights, tau,
                        steering)
     uneven = run_uneven(args, dev, hbm) if (rank == 0 and not args.no_uneven) else None
+    learned = run_learned(args, dev, hbm) if (rank == 0 and not args.no_learned) else None
+    precision = run_precision(args, dev, hbm, tf) if (rank == 0 and not args.no_precision) else None
     standin = library_standin(plan, d_s[0], d_sc[0], kernels["sf_eig_kernel"]["ms"], dev)
 
     line = {
@@ -348,6 +350,8 @@ def run_ours(args, world, rank):
         "e2e": e2e,
         "null_depth_db": nulls,
         "uneven_batch": uneven,
+        "learned_proposer": learned,
+        "precision_form": precision,
         "library_standin": standin,
         "gpu_launches": 3 * args.steps,
         "clocks": clk,
@@ -361,14 +365,18 @@ UNEVEN = {"workload": "uneven_subarray_batch", "units": 8192, "antennas": [16, 3
           "launch": "CUDA graph: persistent correlator + eigensolver size classes + persistent beamformer"}
 
 
-def synth_uneven_on_device(bt, receivers, T, seed, dev):
-    """Seeded synthetic units of the uneven batch, made on the device (5.7 GB
-    of int8 would take minutes in numpy): noise clip(round(N(0, 16^2))) plus
-    0..4 narrowband interferers per unit at INR U[5, 30] dB."""
+def synth_uneven_on_device(bt, receivers, T, seed, dev, steering_units=()):
+    """Seeded synthetic units of a batch, made on the device (gigabytes of
+    int8 would take minutes in numpy): noise clip(round(N(0, 16^2))) plus
+    0..4 narrowband interferers per unit at INR U[5, 30] dB.  Returns the
+    samples and, for the units in steering_units, their interferers' steering
+    vectors (a list of [R][Pol] complex arrays per unit)."""
     import torch
     g = torch.Generator(device=dev)
     g.manual_seed(seed)
     samples = torch.empty(bt.totals["samples"], dtype=torch.int8, device=dev)
+    want = set(int(u) for u in steering_units)
+    steer = {u: [] for u in want}
     recv = np.asarray(receivers)
     t = torch.arange(T, device=dev, dtype=torch.float32)
     for R in sorted(set(recv.tolist())):
@@ -384,6 +392,10 @@ def synth_uneven_on_device(bt, receivers, T, seed, dev):
                 a = torch.complex(torch.randn((n, R, 2), generator=g, device=dev),
                                   torch.randn((n, R, 2), generator=g, device=dev))
                 a = a / torch.linalg.vector_norm(a, dim=1, keepdim=True)
+                on = (n_int > k).cpu().numpy()
+                for j, u in enumerate(us):
+                    if int(u) in want and on[j]:
+                        steer[int(u)].append(a[j].cpu().numpy().astype(np.complex128))
                 f0 = torch.rand(n, generator=g, device=dev) * 0.9 - 0.45
                 ph = torch.rand(n, generator=g, device=dev) * 2 * np.pi
                 ang = 2 * np.pi * f0[:, None] * t[None] + ph[:, None]  # [n][T]
@@ -397,6 +409,8 @@ def synth_uneven_on_device(bt, receivers, T, seed, dev):
             o = int(bt.layout["samples"][us[0]])
             samples[o:o + x.numel()] = x.reshape(-1)
             assert int(bt.layout["samples"][us[-1]]) == o + (n - 1) * T * R * 4
+    if want:
+        return samples, steer
     return samples
 
 
@@ -511,6 +525,309 @@ def run_uneven(args, dev, hbm):
                        "matrices_per_s": round(2 * n_units / (stages["eig"] / 1e3))}},
            "autotune": tuned.get("choice"), "autotune_ms": tuned.get("ms"),
            "oracle_checked_units": checked, "gpu_launches_per_step": 5}
+    bt.close()
+    return out
+
+
+LEARNED = {"workload": "learned_subspace_proposer", "antennas": 36, "polarizations": 2,
+           "covariances_per_batch": 8192, "samples_per_integration": 4096, "beams": 8, "beam_slots": 2,
+           "interferers": "0-4 per channel", "inr_db": [5.0, 30.0], "mlp": "1344-512-512-288 (bf16, ReLU)",
+           "training_covariances": 1000000, "training_samples_per_integration": 1024,
+           "rayleigh_ritz_iterations": 3, "fallback_residual": "1e-3 ||R||", "k_rule": "lambda > 10 x noise floor"}
+
+
+def run_learned(args, dev, hbm):
+    """The learned-subspace-proposer workload: train the MLP on 10^6
+    pipeline-generated covariances, then run 8192 covariances (4096 channels x
+    2 pols, 36 antennas, T = 4096) through the plain chain and the learned chain
+    (warm-started Rayleigh-Ritz, residual-gated fallback), timing both from CUDA
+    graphs and comparing their null depths with the FP64 full eigensolve."""
+    import torch
+    import sfgb
+    import sf_oracle as orc
+    from sfgb import proposer as prop
+    F_, RPP_, TP_ = 4, 9, 64
+    R_ = F_ * RPP_
+    C_ = LEARNED["covariances_per_batch"] // 2
+    P_ = LEARNED["samples_per_integration"] // TP_
+    n_train = LEARNED["training_covariances"]
+    t0 = time.perf_counter()
+    q = prop.Proposer(R_, 512, 8192)
+    q.init_params(seed=0)
+    x, t, w = prop.make_training_set(n_train, q, F=F_, Rpp=RPP_, Tp=TP_, P=LEARNED["training_samples_per_integration"] // TP_,
+                                     chunk_channels=4096, seed=1, dev=dev)
+    t_gen = time.perf_counter() - t0
+    epochs = args.learned_epochs
+    hist = prop.train(q, x, t, w, epochs=epochs, batch=8192, lr=1e-3)
+    t_train = time.perf_counter() - t0 - t_gen
+    del x, t, w
+    torch.cuda.empty_cache()
+    # the test batch
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(12345)
+    samples, steer = prop.synth_packets_on_device(C_, F_, TP_, RPP_, P_, gen, dev)
+    scales = torch.ones((C_, P_ + 2, R_, 2), dtype=torch.int16, device=dev)
+    rng = np.random.default_rng(3)
+    ph = rng.uniform(0, 2 * np.pi, size=(C_, 2, B, R_))
+    weights = np.stack([np.cos(ph), np.sin(ph)], axis=-1).astype(np.float16)
+    plan = sfgb.Plan(C_, F_, TP_, R_, RPP_, P_, B)
+    plan.set_weights(weights)
+    stream = torch.cuda.Stream(device=dev)
+    vis = torch.empty(plan.vis_shape(), dtype=torch.int32, device=dev)
+    ev = torch.empty((C_, 2, R_), dtype=torch.float32, device=dev)
+    cnt_p = torch.empty((C_, 2), dtype=torch.int32, device=dev)
+    cnt_l = torch.empty((C_, 2), dtype=torch.int32, device=dev)
+    beams = torch.empty(plan.beams_shape(2), dtype=torch.float16, device=dev)
+    weff = torch.empty((C_, 2, 2 * B, R_, 2), dtype=torch.float32, device=dev)
+    fb = torch.zeros(1, dtype=torch.int32, device=dev)
+    KR, DELTA, NIT, TOL = sfgb.SF_K_NOISE_FLOOR, 10.0, LEARNED["rayleigh_ritz_iterations"], 1e-3
+    plan.correlate(samples, scales, sfgb.SF_WINDOW_ALIGNED, vis, stream=stream)
+    plan.covariance_eig(vis, sfgb.SF_EIG_SAME_POL_WHITENED, KR, DELTA, False, None, None, cnt_p, None, stream=stream)
+    plan.effective_weights(weff, stream=stream)
+    stream.synchronize()
+    w_plain = weff.cpu().numpy().astype(np.float64)
+    plan.covariance_eig_learned(q, vis, KR, DELTA, NIT, TOL, counts=cnt_l, fallback_count=fb, stream=stream)
+    plan.effective_weights(weff, stream=stream)
+    stream.synchronize()
+    rc, bits = plan.status(stream)
+    if rc != 0:
+        raise RuntimeError(f"learned chain: device status 0x{bits:x}")
+    w_learn = weff.cpu().numpy().astype(np.float64)
+    n_fb = int(fb.item())
+    # FP64 reference weights from the (exact) visibilities: LAPACK on the whitened covariances
+    sh = orc.Shape(C_, F_, TP_, R_, RPP_, P_, B)
+    v = vis.cpu().numpy()
+    vc = orc.scaled_visibilities(sh, v, orc.receiver_factors(sh))
+    wc = weights.astype(np.float64)
+    wc = wc[..., 0] + 1j * wc[..., 1]
+    st = steer.cpu().numpy()
+    resp = {"fp64": [[], []], "plain": [[], []], "learned": [[], []]}
+    k_fp64 = np.zeros((C_, 2), np.int32)
+    for p in range(2):
+        m = orc.unpack_hermitian(sh, vc, p, p)
+        mw = m / np.sqrt(np.einsum("cii->ci", m).real[:, :, None] * np.einsum("cjj->cj", m).real[:, None, :])
+        lam, vec = np.linalg.eigh(mw)
+        s = np.sqrt(np.maximum(np.einsum("cii->ci", m).real, 1e-10))
+        for c in range(C_):
+            k = orc.detect_k_noise_floor(lam[c], DELTA)
+            k_fp64[c, p] = k
+            u = orc.unwhiten_normalize(vec[c], s[c])
+            wp = wc[c, p] @ orc.null_projection(u, k)
+            for a in st[c]:
+                ap = a[:, p]
+                if not np.any(ap):
+                    continue
+                for name, w0, w1 in (("fp64", wc[c, p], wp),
+                                     ("plain", w_plain[c, p, :B, :, 0] + 1j * w_plain[c, p, :B, :, 1],
+                                      w_plain[c, p, B:, :, 0] + 1j * w_plain[c, p, B:, :, 1]),
+                                     ("learned", w_learn[c, p, :B, :, 0] + 1j * w_learn[c, p, :B, :, 1],
+                                      w_learn[c, p, B:, :, 0] + 1j * w_learn[c, p, B:, :, 1])):
+                    resp[name][0].append(np.abs(w0 @ ap) ** 2)
+                    resp[name][1].append(np.abs(w1 @ ap) ** 2)
+    depth = {k: round(float(10 * np.log10(np.sum(np.concatenate(r[1])) / np.sum(np.concatenate(r[0])))), 2)
+             for k, r in resp.items()}
+    # timings: eigen stage and whole chain, plain vs learned, CUDA-graph replays
+    def graph_ms(fn, reps=10):
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            fn()
+        with torch.cuda.stream(stream):
+            g.replay()
+            stream.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                g.replay()
+            e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+    eig_plain = graph_ms(lambda: plan.covariance_eig(vis, sfgb.SF_EIG_SAME_POL_WHITENED, KR, DELTA, False, None, None,
+                                                     cnt_p, None, stream=stream))
+    eig_learn = graph_ms(lambda: plan.covariance_eig_learned(q, vis, KR, DELTA, NIT, TOL, counts=cnt_l,
+                                                             stream=stream))
+    chain_plain = graph_ms(lambda: plan.run_adaptive(samples, scales, KR, DELTA, False, vis, None, None, cnt_p, beams,
+                                                     stream=stream))
+    chain_learn = graph_ms(lambda: plan.run_adaptive_learned(q, samples, scales, KR, DELTA, NIT, TOL, vis, cnt_l,
+                                                             beams, stream=stream))
+    rc, bits = plan.status(stream)
+    if rc != 0:
+        raise RuntimeError(f"learned chain: device status 0x{bits:x} after timing")
+    plan.close()
+    q.close()
+    return {"config": LEARNED, "training": {"covariances": n_train, "epochs": epochs,
+                                            "loss_first_last": [round(hist[0], 5), round(hist[-1], 5)],
+                                            "generation_s": round(t_gen, 2), "training_s": round(t_train, 2)},
+            "value": round(C_ / (chain_learn / 1e3), 1), "unit": UNIT,
+            "plain_value": round(C_ / (chain_plain / 1e3), 1),
+            "chain_ms": {"plain": round(chain_plain, 4), "learned": round(chain_learn, 4),
+                         "speedup": round(chain_plain / chain_learn, 3)},
+            "eig_stage_ms": {"plain": round(eig_plain, 4), "learned": round(eig_learn, 4),
+                             "speedup": round(eig_plain / eig_learn, 3)},
+            "fallback_fraction": round(n_fb / (2 * C_), 4),
+            "null_depth_db": dict(depth, learned_minus_fp64=round(depth["learned"] - depth["fp64"], 2),
+                                  plain_minus_fp64=round(depth["plain"] - depth["fp64"], 2)),
+            "k_agreement": {"learned_vs_fp64": round(float(np.mean(cnt_l.cpu().numpy() == k_fp64)), 4),
+                            "plain_vs_fp64": round(float(np.mean(cnt_p.cpu().numpy() == k_fp64)), 4)}}
+
+
+PRECISION = {"workload": "precision_256_antennas", "antennas": 256, "polarizations": 2, "channels": 1024,
+             "samples_per_integration": 8192, "beams": 64, "beam_slots": 2, "interferers": "0-4 per channel",
+             "inr_db": [5.0, 30.0], "k_rule": "lambda > 10 x median",
+             "eigensolver": "fp32 top-K + FP64 Rayleigh-Ritz refinement (2 steps) + FP64 orthogonal re-projection",
+             "beam_precisions": ["fp16", "bf16", "e4m3 (samples rounded)", "e4m3 split (samples exact)"]}
+
+
+def round_e4m3(x):
+    """Round to the nearest e4m3 value (4 exponent bits, bias 7, 3 mantissa
+    bits, subnormals below 2^-6, saturated at +-448)."""
+    a = np.abs(x)
+    e = np.floor(np.log2(np.maximum(a, 1e-30)))
+    e = np.maximum(e, -6.0)
+    q = 2.0 ** (e - 3)
+    r = np.minimum(np.round(a / q) * q, 448.0)
+    return np.sign(x) * r
+
+
+def quantize_weights(w, precision):
+    """The weights the beamformer's tensor cores multiply: fp16, bf16 or
+    e4m3 of w / s with the per-beam scale s = max(|re|, |im|) / 448 (returned
+    multiplied back by s)."""
+    import torch
+    if precision == "fp16":
+        return w.real.astype(np.float16).astype(np.float64) + 1j * w.imag.astype(np.float16).astype(np.float64)
+    if precision == "bf16":
+        f = lambda v: torch.as_tensor(v).to(torch.bfloat16).to(torch.float64).numpy()
+        return f(w.real) + 1j * f(w.imag)
+    s = np.maximum(np.abs(w.real), np.abs(w.imag)).max(axis=-1, keepdims=True) / 448.0
+    s = np.where(s > 0, s, 1.0)
+    return (round_e4m3(w.real / s) + 1j * round_e4m3(w.imag / s)) * s
+
+
+def run_precision(args, dev, hbm, tf):
+    """The precision workload: 1024 channels of 256 antennas, 8192 samples, 64
+    beams x 2 slots; FP32 eigensolver with FP64 refinement and re-projection;
+    beams in fp16, bf16 and e4m3 (rounded and split samples).  Reports stage
+    times, the tensor-core roofline of the correlator and beamformer, and the
+    beam, null-depth and eigenvalue errors against the FP64 oracle on a sample
+    of channels."""
+    import torch
+    import sfgb
+    import sf_oracle as orc
+    C4, R4, T4, B4 = PRECISION["channels"], PRECISION["antennas"], PRECISION["samples_per_integration"], PRECISION["beams"]
+    recv = np.full(C4, R4, np.int32)
+    bt = sfgb.Batch(recv, T4, B4)
+    rng = np.random.default_rng(21)
+    ws = []
+    for _ in range(C4):
+        ph = rng.uniform(0, 2 * np.pi, size=(2, B4, R4))
+        ws.append(np.stack([np.cos(ph), np.sin(ph)], axis=-1).astype(np.float16))
+    bt.set_weights(bt.pack_weights(ws))
+    sample_units = [0, 1, 2, 3]
+    samples, steer = synth_uneven_on_device(bt, recv, T4, 31, dev, steering_units=sample_units)
+    stream = torch.cuda.Stream(device=dev)
+    vis = torch.empty(bt.totals["vis"], dtype=torch.int32, device=dev)
+    ev = torch.empty(bt.totals["evals"], dtype=torch.float32, device=dev)
+    cnt = torch.empty((C4, 2), dtype=torch.int32, device=dev)
+    beams = torch.empty(2 * bt.totals["beams"], dtype=torch.float16, device=dev)
+    KR, DELTA = sfgb.SF_K_NOISE_FLOOR, 10.0
+
+    def graph_ms(fn, reps=3):
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            fn()
+        with torch.cuda.stream(stream):
+            g.replay()
+            stream.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                g.replay()
+            e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    bt.set_precision(sfgb.SF_BEAM_FP16, 2, True)
+    corr_ms = graph_ms(lambda: bt.correlate(samples, vis, stream=stream))
+    eig_ms = graph_ms(lambda: bt.covariance_eig(vis, KR, DELTA, False, ev, cnt, stream=stream))
+    bt.set_precision(sfgb.SF_BEAM_FP16, 0, True)
+    eig0_ms = graph_ms(lambda: bt.covariance_eig(vis, KR, DELTA, False, ev, cnt, stream=stream))
+    names = {sfgb.SF_BEAM_FP16: "fp16", sfgb.SF_BEAM_BF16: "bf16", sfgb.SF_BEAM_E4M3: "e4m3",
+             sfgb.SF_BEAM_E4M3_SPLIT: "e4m3_split"}
+    # FP64 reference of the sampled channels (first 1024 samples of their beams)
+    ts = 1024
+    refs = {}
+    v_host = None
+    out = {"config": PRECISION, "stages_ms": {"corr": round(corr_ms, 4), "eig_fp32_refine64": round(eig_ms, 4),
+                                              "eig_fp32_rayleigh_ritz64_only": round(eig0_ms, 4)},
+           "beams": {}}
+    flops_corr = 8.0 * (R4 * (R4 + 1) / 2) * 4 * T4 * C4
+    flops_beam = 8.0 * (2 * B4) * R4 * 2 * T4 * C4
+    for prec, name in names.items():
+        bt.set_precision(prec, 2, True)
+        bt.covariance_eig(vis, KR, DELTA, False, ev, cnt, stream=stream)
+        beam_ms = graph_ms(lambda: bt.beamform(samples, beams, stream=stream))
+        stream.synchronize()
+        rc, bits = bt.status(stream)
+        if rc != 0:
+            raise RuntimeError(f"precision batch ({name}): device status 0x{bits:x}")
+        y = beams.cpu().numpy()
+        k = cnt.cpu().numpy()
+        if v_host is None:
+            v_host = vis.cpu().numpy()
+            e_host = ev.cpu().numpy()
+            resid, ritz = bt.precision_report(stream)
+            weff = bt.effective_weights(stream)
+        err_num = err_den = 0.0
+        depth = {"q": [[], []], "fp64": [[], []]}
+        for u in sample_units:
+            if u not in refs:
+                o = int(bt.layout["samples"][u])
+                x = samples[o:o + T4 * R4 * 4].cpu().numpy().reshape(T4, R4, 2, 2)
+                # beams of the first ts samples only (the oracle's beam sum over all 8192 is slow)
+                ref = orc.unit_chain(x, ws[u], "fixed", k_fixed=k[u], orthogonal=True, beam_samples=ts)
+                refs[u] = (ref, x)
+            ref, x = refs[u]
+            if not np.array_equal(bt.unit_vis(v_host, u), ref["vis"]):
+                raise RuntimeError(f"precision batch: unit {u} visibilities differ from the oracle")
+            yb = bt.unit_beams(y, u)[:, :, :ts].astype(np.float64)
+            yb = yb[..., 0] + 1j * yb[..., 1]
+            yr = ref["beams"][:, :, :ts]
+            err_num += float(np.sum(np.abs(yb - yr) ** 2))
+            err_den += float(np.sum(np.abs(yr) ** 2))
+            wq = quantize_weights(weff[u], name.split("_")[0] if name != "e4m3_split" else "e4m3")
+            for a in steer[u]:
+                for p in range(2):
+                    for key, w in (("q", wq[p]), ("fp64", ref["w_eff"][p])):
+                        depth[key][0].append(np.abs(w[:B4] @ a[:, p]) ** 2)
+                        depth[key][1].append(np.abs(w[B4:] @ a[:, p]) ** 2)
+        dq = 10 * np.log10(np.sum(depth["q"][1]) / np.sum(depth["q"][0])) if depth["q"][0] else None
+        d64 = 10 * np.log10(np.sum(depth["fp64"][1]) / np.sum(depth["fp64"][0])) if depth["fp64"][0] else None
+        out["beams"][name] = {"beam_ms": round(beam_ms, 4),
+                              "chain_ms": round(corr_ms + eig_ms + beam_ms, 4),
+                              "value": round(C4 / ((corr_ms + eig_ms + beam_ms) / 1e3), 1), "unit": UNIT,
+                              "beam_rel_rms_error": round(float(np.sqrt(err_num / err_den)), 6),
+                              "null_depth_db": None if dq is None else round(float(dq), 2),
+                              "null_depth_fp64_db": None if d64 is None else round(float(d64), 2),
+                              "beam_tflops": round(flops_beam / (beam_ms / 1e3) / 1e12, 1)}
+    # eigenvalue errors of the sampled channels: fp32 eigensolver and FP64 Ritz values vs LAPACK
+    ev_err = rz_err = 0.0
+    for u in sample_units:
+        ref = refs[u][0]
+        nrm = np.abs(ref["evals"]).max(axis=-1, keepdims=True)
+        ev_err = max(ev_err, float(np.max(np.abs(bt.unit_evals(e_host, u) - ref["evals"]) / nrm)))
+        for p in range(2):
+            kk = int(k[u, p])
+            if kk:
+                top = ref["evals"][p][::-1][:kk]
+                rz_err = max(rz_err, float(np.max(np.abs(ritz[u, p, :kk] - top) / top[0])))
+    out["eigen"] = {"fp32_eigenvalue_max_error_rel_norm": ev_err, "fp64_ritz_max_error_rel": rz_err,
+                    "residual_fp32_median": float(np.median(resid[:, :, 0][k > 0])) if np.any(k > 0) else None,
+                    "residual_refined64_median": float(np.median(resid[:, :, 1][k > 0])) if np.any(k > 0) else None,
+                    "k_histogram": np.bincount(k.reshape(-1), minlength=5)[:8].tolist()}
+    out["roofline"] = {"corr": {"bound": "tensor", "achieved": round(flops_corr / (corr_ms / 1e3) / 1e12, 1),
+                                "peak": tf, "unit": "TFLOP/s",
+                                "frac": round(flops_corr / (corr_ms / 1e3) / 1e12 / tf, 4)}}
+    out["sampled_channels"] = sample_units
     bt.close()
     return out
 
@@ -825,6 +1142,9 @@ def main():
     ap.add_argument("--ref-channels", type=int, default=384)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven sub-array batch workload")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-proposer workload")
+    ap.add_argument("--no-precision", action="store_true", help="skip the 256-antenna precision workload")
+    ap.add_argument("--learned-epochs", type=int, default=12)
     ap.add_argument("--channels", type=int, default=C,
                     help="channels per integration (default: the 384-channel workload)")
     ap.add_argument("--only-stage", choices=["corr", "eig", "beam", "packet_spectra", "beam_spectra"],

@@ -36,6 +36,8 @@
 // 2-3 and 8-15 converters.  Every mbarrier wait is bounded and reports
 // through the status word.
 #include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp8.h>
 #include <cudaTypedefs.h>
 
 #include <algorithm>
@@ -99,6 +101,44 @@ __device__ __forceinline__ void int8x4_to_half(uint32_t word, uint32_t &o0, uint
   o1 = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4342)), bias));
 }
 
+// Beam operand precisions (SF_BEAM_*): fp16 or bf16 samples and weights
+// (kind::f16, exact samples); e4m3 samples and weights (kind::f8f6f4, samples
+// rounded to e4m3); e4m3 weights with exact samples split as
+// x = 16 (x >> 4) + (x & 15), both parts exact in e4m3, two MMAs per K step.
+enum : int { OP_F16 = 0, OP_BF16 = 1, OP_E4M3 = 2, OP_E4M3_SPLIT = 3 };
+
+__device__ __forceinline__ uint32_t bf16x2_of(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t *>(&v);
+}
+
+// two floats -> two e4m3 bytes (round to nearest, saturate to the finite range)
+__device__ __forceinline__ uint32_t e4m3x2_of(float lo, float hi) {
+  const __nv_fp8x2_storage_t v = __nv_cvt_float2_to_fp8x2(make_float2(lo, hi), __NV_SATFINITE, __NV_E4M3);
+  return static_cast<uint32_t>(v);
+}
+
+// four int8 of a word -> four e4m3 bytes of f(x) for f = rounding (mode 0),
+// 16 (x >> 4) (mode 1) or x & 15 (mode 2); the last two are exact in e4m3
+__device__ __forceinline__ uint32_t int8x4_to_e4m3(uint32_t word, int mode) {
+  float v[4];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    const int x = static_cast<int8_t>((word >> (8 * b)) & 0xFFu);
+    v[b] = mode == 0 ? static_cast<float>(x) : (mode == 1 ? static_cast<float>(16 * (x >> 4)) : static_cast<float>(x & 15));
+  }
+  return e4m3x2_of(v[0], v[1]) | (e4m3x2_of(v[2], v[3]) << 16);
+}
+
+SF_DEVICE void umma_f8(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
 struct BatchArgs {
   CUtensorMap tmap[SF_BATCH_MAX_CLASSES];  // int8 [rows][4R bytes] per size class
   const SfBatchUnit *units;
@@ -109,15 +149,18 @@ struct BatchArgs {
   int32_t *vis;
   const float2 *weff;    // [unit][Pol][NB][R] at unit.weff_off
   __half2 *beams;        // [unit][Pol][NB][T] at unit.beam_off
-  int NB, BN;            // beams per pol written, beam MMA N = round16(4 NB)
+  int NB, BN;            // beams per pol written (all slots), beam MMA N = round16(4 NBG)
+  int NBG;               // beams per pol of one beam item (a group of the NB)
+  const float *scales;   // fp8 operands: per-beam weight scale [unit][Pol][NB] (weights / scale in e4m3)
   int sa, ni, nf;        // atoms per slab, int8 / fp16 ring depths
   uint32_t wtile_bytes;  // beam weight tile (katoms_max x BN x 128 B)
   uint32_t tmem_cols;
   uint32_t *status;
 };
 
-template <bool BEAM>
+template <bool BEAM, int OP>
 __global__ void __launch_bounds__(NTHREADS, 1) sf_batch_kernel(const __grid_constant__ BatchArgs a) {
+  constexpr bool F8 = OP == OP_E4M3 || OP == OP_E4M3_SPLIT;
   extern __shared__ __align__(16) uint8_t smem[];
   Header &h = *reinterpret_cast<Header *>(smem);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -206,7 +249,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_batch_kernel(const __grid_cons
           failed |= !mbar_wait(&h.w_full, (oi - first) & 1, abort_flag, SUSPEND);
           tc_fence_after();
         }
-        const uint32_t idesc = BEAM ? umma_idesc_f16_f32(128, a.BN)
+        // beam: K-major A and B; bf16 operands set the format fields (bits 7-9, 10-12), e4m3 is format 0
+        // of kind::f8f6f4; correlator: both operands MN-major (bits 15, 16)
+        const uint32_t idesc = BEAM ? (umma_idesc_f16_f32(128, a.BN) | (OP == OP_BF16 ? (1u << 7) | (1u << 10) : 0u))
                                     : (umma_idesc_f16_f32(it.m, it.n) | (1u << 15) | (1u << 16));
         for (int st = 0; st < a.nst; ++st) {
           uint32_t abuf = 0, dacc = 0;
@@ -232,7 +277,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_batch_kernel(const __grid_cons
             tc_fence_after();
             const uint32_t slab = f16_addr + s * f16_slab;
             if (ok && !*abort_flag) {
-              if (BEAM) {
+              if (BEAM && !F8) {
                 const int na = slab_atoms(it, gs);
                 for (int k = 0; k < na; ++k) {
                   const uint64_t ad = desc_sw128(slab + k * ATOM, 16, 1024);
@@ -241,6 +286,23 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_batch_kernel(const __grid_cons
                   for (int ks = 0; ks < 4; ++ks)
                     umma_f16(dacc, ad + ((ks * 32) >> 4), bd + ((ks * 32) >> 4), idesc,
                              (gs == 0 && k == 0 && ks == 0) ? 0u : 1u);
+                }
+              } else if (BEAM) {
+                // e4m3 atoms of 128 u (two int8 boxes each): [hi (or rounded) atoms][lo atoms]
+                const int nf8 = (slab_atoms(it, gs) + 1) >> 1;
+                const int half = a.sa >> 1;
+                for (int k = 0; k < nf8; ++k) {
+                  const uint64_t bd = desc_sw128(w_addr + (gs * half + k) * (a.BN * 128), 16, 1024);
+                  const uint64_t ad = desc_sw128(slab + k * ATOM, 16, 1024);
+#pragma unroll
+                  for (int ks = 0; ks < 4; ++ks)
+                    umma_f8(dacc, ad + ((ks * 32) >> 4), bd + ((ks * 32) >> 4), idesc,
+                            (gs == 0 && k == 0 && ks == 0) ? 0u : 1u);
+                  if (OP == OP_E4M3_SPLIT) {
+                    const uint64_t al = desc_sw128(slab + (half + k) * ATOM, 16, 1024);
+#pragma unroll
+                    for (int ks = 0; ks < 4; ++ks) umma_f8(dacc, al + ((ks * 32) >> 4), bd + ((ks * 32) >> 4), idesc, 1u);
+                  }
                 }
               } else {
                 const uint64_t ad = desc_sw128(slab, ATOM, 1024);
@@ -285,7 +347,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_batch_kernel(const __grid_cons
           tc_fence_after();
           const int t = st * BT + q4 * 32 + lane;
           __half2 *dst = a.beams + un.beam_off + t;
-          const int ncplx = 2 * a.NB;  // output rows (pol, beam)
+          // this item's beams: c0 .. c0 + n - 1 of every pol; tile column pair (pol, local beam)
           for (int cb = 0; cb < a.BN / 16; ++cb) {
             uint32_t v[16];
             tmem_ld16(tq + buf * a.BN + cb * 16, v);
@@ -293,9 +355,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_batch_kernel(const __grid_cons
             if (ok) {
 #pragma unroll
               for (int e2 = 0; e2 < 8; ++e2) {
-                const int col = cb * 8 + e2;
-                if (col < ncplx)
-                  dst[(size_t)col * a.T] = __floats2half2_rn(__uint_as_float(v[2 * e2]), __uint_as_float(v[2 * e2 + 1]));
+                const int lo = cb * 8 + e2;
+                const int pn = lo / a.NBG, mn = lo - pn * a.NBG;
+                if (pn < 2 && mn < it.n) {
+                  const int col = pn * a.NB + it.c0 + mn;
+                  const float sc = F8 ? a.scales[((size_t)it.unit * 2 + pn) * a.NB + it.c0 + mn] : 1.0f;
+                  dst[(size_t)col * a.T] =
+                      __floats2half2_rn(sc * __uint_as_float(v[2 * e2]), sc * __uint_as_float(v[2 * e2 + 1]));
+                }
               }
             }
           }
@@ -371,27 +438,34 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_batch_kernel(const __grid_cons
         failed |= !ok;
         if (ok) {
           const int R = un.R;
-          const int nchunk = it.natoms * 8;
+          // 16-byte chunks per row: 8 per 64-u atom (16-bit), 8 per 128-u atom (e4m3)
+          const int vper = F8 ? 16 : 8;  // u values per chunk
+          const int natw = F8 ? (it.natoms + 1) >> 1 : it.natoms;
+          const int nchunk = natw * 8;
           for (int task = ct; task < a.BN * nchunk; task += NCT) {
             const int n = task / nchunk, ch = task - n * nchunk;
             const int atom = ch >> 3, cc = ch & 7;
-            const int pn = n / (2 * a.NB), mn = (n >> 1) - pn * a.NB, cn = n & 1;
+            const int pn = n / (2 * a.NBG), mn = (n >> 1) - pn * a.NBG, cn = n & 1;
+            const bool beam_ok = pn < 2 && mn < it.n;
+            const float inv = F8 && beam_ok ? 1.0f / a.scales[((size_t)it.unit * 2 + pn) * a.NB + it.c0 + mn] : 1.0f;
+            float vals[16];
+#pragma unroll
+            for (int dd = 0; dd < 16; ++dd) {
+              vals[dd] = 0.0f;
+              if (dd >= vper) continue;
+              const int uu = atom * (8 * vper) + cc * vper + dd;
+              const int r = uu >> 2, pu = (uu >> 1) & 1, cu = uu & 1;
+              if (beam_ok && uu < 4 * R && pu == pn) {
+                const float2 w = a.weff[un.weff_off + ((size_t)pn * a.NB + it.c0 + mn) * R + r];
+                vals[dd] = (cn == 0 ? (cu == 0 ? w.x : -w.y) : (cu == 0 ? w.y : w.x)) * inv;
+              }
+            }
             uint32_t pk[4];
 #pragma unroll
             for (int qq = 0; qq < 4; ++qq) {
-              float vals[2];
-#pragma unroll
-              for (int dd = 0; dd < 2; ++dd) {
-                const int uu = atom * 64 + cc * 8 + qq * 2 + dd;
-                const int r = uu >> 2, pu = (uu >> 1) & 1, cu = uu & 1;
-                float v = 0.0f;
-                if (pn < 2 && uu < 4 * R && pu == pn) {
-                  const float2 w = a.weff[un.weff_off + ((size_t)pn * a.NB + mn) * R + r];
-                  v = cn == 0 ? (cu == 0 ? w.x : -w.y) : (cu == 0 ? w.y : w.x);
-                }
-                vals[dd] = v;
-              }
-              pk[qq] = u32_of(__floats2half2_rn(vals[0], vals[1]));
+              if (OP == OP_F16) pk[qq] = u32_of(__floats2half2_rn(vals[2 * qq], vals[2 * qq + 1]));
+              else if (OP == OP_BF16) pk[qq] = bf16x2_of(vals[2 * qq], vals[2 * qq + 1]);
+              else pk[qq] = e4m3x2_of(vals[4 * qq], vals[4 * qq + 1]) | (e4m3x2_of(vals[4 * qq + 2], vals[4 * qq + 3]) << 16);
             }
             *reinterpret_cast<uint4 *>(w_ptr + atom * (a.BN * 128) + n * 128 + ((cc ^ (n & 7)) << 4)) =
                 make_uint4(pk[0], pk[1], pk[2], pk[3]);
@@ -407,20 +481,51 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_batch_kernel(const __grid_cons
           bool ok = mbar_wait(&h.i8_full[si], (g / a.ni) & 1u, abort_flag, SUSPEND);
           ok = ok && mbar_wait(&h.f16_empty[sf], ((g / a.nf) & 1u) ^ 1u, abort_flag, SUSPEND);
           failed |= !ok;
-          if (ok) {
+          if (ok && !F8) {
             const int na = slab_atoms(it, gs);
             // task = (atom slot, sample t, 16-byte quarter q of the atom's 64 bytes)
             for (int task = ct; task < na * BT * 4; task += NCT) {
               const int k = task >> 9, t = (task >> 2) & (BT - 1), q = task & 3;
               const uint4 v = lds128(i8s + si * i8_slab + k * IATOM + t * 64 + q * 16);
               uint32_t o[8];
-              int8x4_to_half(v.x, o[0], o[1]);
-              int8x4_to_half(v.y, o[2], o[3]);
-              int8x4_to_half(v.z, o[4], o[5]);
-              int8x4_to_half(v.w, o[6], o[7]);
+              if (OP == OP_BF16) {
+                const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                  const float x0 = static_cast<float>(static_cast<int8_t>(w4[b] & 0xFF));
+                  const float x1 = static_cast<float>(static_cast<int8_t>((w4[b] >> 8) & 0xFF));
+                  const float x2 = static_cast<float>(static_cast<int8_t>((w4[b] >> 16) & 0xFF));
+                  const float x3 = static_cast<float>(static_cast<int8_t>(w4[b] >> 24));
+                  o[2 * b] = bf16x2_of(x0, x1);
+                  o[2 * b + 1] = bf16x2_of(x2, x3);
+                }
+              } else {
+                int8x4_to_half(v.x, o[0], o[1]);
+                int8x4_to_half(v.y, o[2], o[3]);
+                int8x4_to_half(v.z, o[4], o[5]);
+                int8x4_to_half(v.w, o[6], o[7]);
+              }
               const uint32_t row = f16s + sf * f16_slab + k * ATOM + t * 128;
               sts128(row + (((2 * q) ^ (t & 7)) << 4), o[0], o[1], o[2], o[3]);
               sts128(row + (((2 * q + 1) ^ (t & 7)) << 4), o[4], o[5], o[6], o[7]);
+            }
+          } else if (ok) {
+            // e4m3: int8 box k fills half (k & 1) of 128-u atom k >> 1 (hi / rounded part), and of atom
+            // sa / 2 + (k >> 1) (lo part, split only); boxes past the unit's atoms are zeros
+            const int na = slab_atoms(it, gs);
+            const int nbox = ((na + 1) >> 1) << 1;
+            const int half = a.sa >> 1;
+            for (int task = ct; task < nbox * BT * 4; task += NCT) {
+              const int k = task >> 9, t = (task >> 2) & (BT - 1), q = task & 3;
+              const uint4 v = k < na ? lds128(i8s + si * i8_slab + k * IATOM + t * 64 + q * 16) : make_uint4(0, 0, 0, 0);
+              const int c = ((k & 1) << 2) + q;  // 16-byte chunk of the 128-byte row
+              const uint32_t row = f16s + sf * f16_slab + (k >> 1) * ATOM + t * 128 + ((c ^ (t & 7)) << 4);
+              const int m0 = OP == OP_E4M3 ? 0 : 1;
+              sts128(row, int8x4_to_e4m3(v.x, m0), int8x4_to_e4m3(v.y, m0), int8x4_to_e4m3(v.z, m0),
+                     int8x4_to_e4m3(v.w, m0));
+              if (OP == OP_E4M3_SPLIT)
+                sts128(row + half * ATOM, int8x4_to_e4m3(v.x, 2), int8x4_to_e4m3(v.y, 2), int8x4_to_e4m3(v.z, 2),
+                       int8x4_to_e4m3(v.w, 2));
             }
           }
           fence_proxy_async_smem();
@@ -532,27 +637,59 @@ cudaError_t sf_batch_launch(const SfBatchLaunch &L, bool beam, const int8_t *sam
   a.weff = weff;
   a.beams = beams;
   a.NB = L.NB;
-  a.BN = ((4 * L.NB + 15) / 16) * 16;
+  a.NBG = L.NBG;
+  a.BN = ((4 * L.NBG + 15) / 16) * 16;
+  a.scales = L.d_scales;
+  const int op = L.beam_op;
+  const bool f8 = op == OP_E4M3 || op == OP_E4M3_SPLIT;
   a.sa = beam ? L.beam_sa : MAX_SA;
   a.ni = beam ? L.beam_ni : L.corr_ni;
   a.nf = beam ? L.beam_nf : L.corr_nf;
-  a.wtile_bytes = beam ? static_cast<uint32_t>(L.max_atoms * a.BN * 128) : 0u;
+  a.wtile_bytes = beam ? static_cast<uint32_t>((f8 ? (L.max_atoms + 1) / 2 : L.max_atoms) * a.BN * 128) : 0u;
   a.tmem_cols = 512;
   a.status = status;
   if (beam && (a.BN > 256 || 2 * a.BN > 512)) return cudaErrorInvalidConfiguration;
+  if (beam && f8 && ((a.sa & 1) || !a.scales)) return cudaErrorInvalidConfiguration;
   const size_t smem = sf_batch_smem_bytes(beam, a.sa, a.ni, a.nf, a.wtile_bytes);
   if (smem > (size_t)sf_device_max_smem()) return cudaErrorInvalidConfiguration;
   const int grid = beam ? L.beam_grid : L.corr_grid;
   if (grid <= 0) return cudaSuccess;
-  if (beam) {
-    e = sf_smem_optin(reinterpret_cast<const void *>(sf_batch_kernel<true>), smem);
-    if (e != cudaSuccess) return e;
-    sf_batch_kernel<true><<<grid, NTHREADS, smem, stream>>>(a);
-  } else {
-    e = sf_smem_optin(reinterpret_cast<const void *>(sf_batch_kernel<false>), smem);
-    if (e != cudaSuccess) return e;
-    sf_batch_kernel<false><<<grid, NTHREADS, smem, stream>>>(a);
-  }
+  const void *fn = nullptr;
+  if (!beam) fn = reinterpret_cast<const void *>(sf_batch_kernel<false, OP_F16>);
+  else if (op == OP_BF16) fn = reinterpret_cast<const void *>(sf_batch_kernel<true, OP_BF16>);
+  else if (op == OP_E4M3) fn = reinterpret_cast<const void *>(sf_batch_kernel<true, OP_E4M3>);
+  else if (op == OP_E4M3_SPLIT) fn = reinterpret_cast<const void *>(sf_batch_kernel<true, OP_E4M3_SPLIT>);
+  else fn = reinterpret_cast<const void *>(sf_batch_kernel<true, OP_F16>);
+  e = sf_smem_optin(fn, smem);
+  if (e != cudaSuccess) return e;
+  if (!beam) sf_batch_kernel<false, OP_F16><<<grid, NTHREADS, smem, stream>>>(a);
+  else if (op == OP_BF16) sf_batch_kernel<true, OP_BF16><<<grid, NTHREADS, smem, stream>>>(a);
+  else if (op == OP_E4M3) sf_batch_kernel<true, OP_E4M3><<<grid, NTHREADS, smem, stream>>>(a);
+  else if (op == OP_E4M3_SPLIT) sf_batch_kernel<true, OP_E4M3_SPLIT><<<grid, NTHREADS, smem, stream>>>(a);
+  else sf_batch_kernel<true, OP_F16><<<grid, NTHREADS, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
+// Per-beam weight scales for e4m3 operands: s = max over receivers of
+// max(|re w|, |im w|) / 448 (the largest finite e4m3), 1 for an all-zero beam.
+__global__ void sf_beam_scales_kernel(const SfBatchUnit *units, const float2 *weff, int n_units, int NB,
+                                      float *scales) {
+  const int row = blockIdx.x * blockDim.y + threadIdx.y;  // (unit, pol, beam)
+  if (row >= n_units * 2 * NB) return;
+  const int unit = row / (2 * NB), pb = row - unit * 2 * NB;
+  const SfBatchUnit un = units[unit];
+  const float2 *w = weff + un.weff_off + (size_t)pb * un.R;
+  float m = 0.0f;
+  for (int r = threadIdx.x; r < un.R; r += 32) m = fmaxf(m, fmaxf(fabsf(w[r].x), fabsf(w[r].y)));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (threadIdx.x == 0) scales[row] = m > 0.0f ? m / 448.0f : 1.0f;
+}
+
+cudaError_t sf_batch_launch_scales(const SfBatchLaunch &L, int n_units, const float2 *weff, float *scales,
+                                   cudaStream_t stream) {
+  const dim3 block(32, 8);
+  const int rows = n_units * 2 * L.NB;
+  sf_beam_scales_kernel<<<(rows + 7) / 8, block, 0, stream>>>(L.d_units, weff, n_units, L.NB, scales);
   return cudaGetLastError();
 }
 

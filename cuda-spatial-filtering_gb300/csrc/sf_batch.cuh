@@ -27,6 +27,7 @@ struct SfBatchItem {
   int m, n;        // correlator MMA M and N
   int row0, c0;    // first Gram row and column (u index)
   int natoms;      // correlator: atoms per slab; beamformer: atoms of the unit (ceil(4R / 64))
+                   // beamformer: m unused, c0 = first beam of the group, n = beams in the group
   int b_slot;      // correlator: slab slot of the first B atom
   uint32_t atoms;  // correlator: global atom index of each slab slot (one byte each)
 };
@@ -45,6 +46,9 @@ struct SfBatchLaunch {
   int corr_grid, beam_grid;
   int corr_ni, corr_nf;            // correlator int8 / fp16 ring depths (slabs of four atoms)
   int beam_sa, beam_ni, beam_nf;   // beamformer atoms per slab and ring depths
+  int NBG;                         // beams per pol of one beamformer item
+  int beam_op;                     // beam operand precision (SF_BEAM_*)
+  const float *d_scales;           // per-beam weight scales of e4m3 operands [unit][Pol][NB]
 };
 
 size_t sf_batch_smem_bytes(bool beam, int sa, int ni, int nf, uint32_t wtile_bytes);
@@ -54,3 +58,5 @@ void sf_batch_schedule(const std::vector<SfBatchItem> &items, const std::vector<
                        std::vector<int> &order);
 cudaError_t sf_batch_launch(const SfBatchLaunch &L, bool beam, const int8_t *samples, int32_t *vis,
                             const float2 *weff, __half2 *beams, uint32_t *status, cudaStream_t stream);
+cudaError_t sf_batch_launch_scales(const SfBatchLaunch &L, int n_units, const float2 *weff, float *scales,
+                                   cudaStream_t stream);

@@ -16,6 +16,11 @@
 #include "sf_common.cuh"
 
 int sf_internal_set_error(int code, const char *msg);
+int sf_refine64_kmax();
+cudaError_t sf_launch_refine64(const SfEigItem *items, int count, const int32_t *vis, const float2 *u32,
+                               const int32_t *counts, const __half2 *weights, float2 *weff,
+                               int B, int steps, int orthogonal, double *ritz, float *resid, uint32_t *status,
+                               cudaStream_t stream);
 
 namespace {
 
@@ -40,6 +45,9 @@ int cuda_fail(cudaError_t e, const char *what) {
   } while (0)
 
 constexpr int N_EIG_GROUPS = 3;  // eigensolver size classes: n <= 32, <= 64, <= 128
+constexpr int MAX_R = 256;       // receivers per unit (above 128: the precision path)
+constexpr int MAX_B_PRECISION = 64;
+constexpr int MAX_NBG = 32;      // beams per pol (all slots) of one beamformer item
 
 template <typename T> int upload(T **dst, const std::vector<T> &src) {
   if (*dst) cudaFree(*dst);
@@ -77,6 +85,19 @@ struct sf_batch {
   uint32_t *d_status = nullptr;
   double corr_conv_weight = 32.0, beam_conv_weight = 32.0;
   std::string tuned;  // the autotuner's last choice (JSON)
+  // precision path: FP32 top-K vectors, FP64 refinement + re-projection, bf16 / e4m3 beams
+  bool precision = false;   // set by sf_batch_set_precision (forced for R > 128 or B > 16)
+  bool needs_precision = false;
+  int refine_steps = 2, orthogonal = 1;
+  float2 *d_u = nullptr;         // FP32 vectors [item][min(n, 64)][n]
+  float2 *d_gA = nullptr;        // working matrices of the n > 128 eigensolver, one per CTA
+  int gA_grid = 0, n_max = 0;
+  double *d_ritz = nullptr;
+  float *d_resid = nullptr;
+  float *d_scales = nullptr;
+  int eig_small_count = 0;  // eig items with n <= 128 come first in the precision order
+  std::vector<SfEigItem> peig_items;
+  SfEigItem *d_peig_items = nullptr;
 };
 
 namespace {
@@ -95,6 +116,12 @@ void free_batch(sf_batch *b) {
   cudaFree(b->d_weff);
   cudaFree(b->d_fixed);
   cudaFree(b->d_status);
+  cudaFree(b->d_u);
+  cudaFree(b->d_gA);
+  cudaFree(b->d_ritz);
+  cudaFree(b->d_resid);
+  cudaFree(b->d_scales);
+  cudaFree(b->d_peig_items);
   for (int g = 0; g < N_EIG_GROUPS; ++g) {
     if (b->side[g]) cudaStreamDestroy(b->side[g]);
     if (b->join[g]) cudaEventDestroy(b->join[g]);
@@ -134,12 +161,12 @@ int sf_batch_create(int32_t n_units, const int32_t *h_receivers, int32_t n_sampl
   if (n_units < 1) return fail(SF_ERR_INVALID_ARGUMENT, "n_units must be >= 1");
   if (n_samples < 128 || n_samples % 128 != 0)
     return fail(SF_ERR_UNSUPPORTED, "n_samples must be a positive multiple of 128 (got %d)", n_samples);
-  if (n_beams < 1 || n_beams > sf_eig_topk_max_b())
-    return fail(SF_ERR_UNSUPPORTED, "n_beams must be in [1, %d]", sf_eig_topk_max_b());
+  if (n_beams < 1 || n_beams > MAX_B_PRECISION)
+    return fail(SF_ERR_UNSUPPORTED, "n_beams must be in [1, %d]", MAX_B_PRECISION);
   for (int u = 0; u < n_units; ++u)
-    if (h_receivers[u] < 4 || h_receivers[u] % 4 != 0 || h_receivers[u] > sf_eig_topk_max_n())
-      return fail(SF_ERR_UNSUPPORTED, "unit %d: receivers must be a multiple of 4 in [4, %d] (got %d)", u,
-                  sf_eig_topk_max_n(), h_receivers[u]);
+    if (h_receivers[u] < 4 || h_receivers[u] % 4 != 0 || h_receivers[u] > MAX_R)
+      return fail(SF_ERR_UNSUPPORTED, "unit %d: receivers must be a multiple of 4 in [4, %d] (got %d)", u, MAX_R,
+                  h_receivers[u]);
   int dev = 0, major = 0, minor = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(SF_ERR_NO_DEVICE, "no CUDA device");
   cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
@@ -210,12 +237,24 @@ int sf_batch_create(int32_t n_units, const int32_t *h_receivers, int32_t n_sampl
     un.beam_off = b->beam_elems;
     b->beam_elems += 2LL * 2 * n_beams * n_samples;
     sf_batch_corr_items(u, R, b->corr_items);
-    SfBatchItem bi{};
-    bi.unit = u;
-    bi.natoms = (4 * R + 63) / 64;
-    b->beam_items.push_back(bi);
-    max_atoms = std::max(max_atoms, bi.natoms);
+    // beamformer items: groups of at most MAX_NBG beams (all slots) per pol
+    const int NB = 2 * n_beams;
+    const int nbg = std::min(NB, MAX_NBG);
+    for (int g0 = 0; g0 < NB; g0 += nbg) {
+      SfBatchItem bi{};
+      bi.unit = u;
+      bi.natoms = (4 * R + 63) / 64;
+      bi.c0 = g0;
+      bi.n = std::min(nbg, NB - g0);
+      b->beam_items.push_back(bi);
+      max_atoms = std::max(max_atoms, bi.natoms);
+    }
+    b->n_max = std::max(b->n_max, R);
   }
+  b->L.NBG = std::min(2 * n_beams, MAX_NBG);
+  b->L.beam_op = SF_BEAM_FP16;
+  b->needs_precision = b->n_max > sf_eig_topk_max_n() || n_beams > sf_eig_topk_max_b();
+  b->precision = b->needs_precision;
   b->L.max_atoms = max_atoms;
   // eigensolver items grouped by size class
   const int limits[N_EIG_GROUPS] = {32, 64, 128};
@@ -243,8 +282,40 @@ int sf_batch_create(int32_t n_units, const int32_t *h_receivers, int32_t n_sampl
     lo = limits[g];
   }
   b->eig_first[N_EIG_GROUPS] = (int)b->eig_items.size();
+  // precision path: every (unit, pol), n <= 128 first, then the larger ones, each with room for
+  // min(n, 64) FP32 eigenvectors
+  {
+    long long ucur = 0;
+    for (int pass = 0; pass < 2; ++pass)
+      for (int u = 0; u < n_units; ++u) {
+        const int R = b->R[u];
+        if ((pass == 0) != (R <= 128)) continue;
+        for (int p = 0; p < 2; ++p) {
+          SfEigItem e{};
+          e.vis_off = b->vis_off[u];
+          e.weight_off = b->weight_off[u] + (long long)p * n_beams * R;
+          e.weff_off = b->units[u].weff_off + (long long)p * 2 * n_beams * R;
+          e.eval_off = b->eval_off[u] + (long long)p * R;
+          e.u_off = ucur;
+          e.n = R;
+          e.pol = p;
+          e.count_idx = 2 * u + p;
+          e.unit = u;
+          b->peig_items.push_back(e);
+          ucur += (long long)std::min(R, 64) * R;
+        }
+      }
+    b->eig_small_count = 0;
+    for (const SfEigItem &e : b->peig_items) b->eig_small_count += e.n <= 128;
+    cudaError_t eu = cudaMalloc(&b->d_u, sizeof(float2) * std::max(1LL, ucur));
+    if (eu != cudaSuccess) {
+      free_batch(b);
+      return cuda_fail(eu, "precision vectors");
+    }
+  }
   for (int g = 0; g < N_EIG_GROUPS; ++g)
-    if (b->eig_nmax[g] > 0 && sf_eig_topk_items_smem(b->eig_nmax[g], n_beams) > (size_t)sf_device_max_smem()) {
+    if (!b->needs_precision && b->eig_nmax[g] > 0 &&
+        sf_eig_topk_items_smem(b->eig_nmax[g], n_beams) > (size_t)sf_device_max_smem()) {
       const int nm = b->eig_nmax[g];
       free_batch(b);
       return fail(SF_ERR_UNSUPPORTED, "%d receivers with %d beams exceed the eigensolver's shared memory", nm,
@@ -262,6 +333,19 @@ int sf_batch_create(int32_t n_units, const int32_t *h_receivers, int32_t n_sampl
   if (!rc) rc = upload(&b->d_corr_items, b->corr_items);
   if (!rc) rc = upload(&b->d_beam_items, b->beam_items);
   if (!rc) rc = upload(&b->d_eig_items, b->eig_items);
+  if (!rc) rc = upload(&b->d_peig_items, b->peig_items);
+  if (!rc) {
+    const int np = (int)b->peig_items.size();
+    cudaError_t ep = cudaMalloc(&b->d_ritz, sizeof(double) * np * sf_refine64_kmax());
+    if (ep == cudaSuccess) ep = cudaMalloc(&b->d_resid, sizeof(float) * np * 2);
+    if (ep == cudaSuccess) ep = cudaMalloc(&b->d_scales, sizeof(float) * n_units * 2 * 2 * n_beams);
+    if (ep == cudaSuccess && b->n_max > 128) {
+      b->gA_grid = std::min(sms, np - b->eig_small_count);
+      ep = cudaMalloc(&b->d_gA, sizeof(float2) * (size_t)b->gA_grid * b->n_max * (b->n_max + 1));
+    }
+    if (ep != cudaSuccess) rc = cuda_fail(ep, "precision buffers");
+    b->L.d_scales = b->d_scales;
+  }
   if (!rc) {
     b->L.d_units = b->d_units;
     b->L.d_corr_items = b->d_corr_items;
@@ -358,6 +442,26 @@ int sf_batch_covariance_eig(sf_batch *b, const int32_t *d_vis, int32_t k_rule, f
   if (!d_vis) return fail(SF_ERR_INVALID_ARGUMENT, "vis is NULL");
   if (k_rule < SF_K_FIXED || k_rule > SF_K_NOISE_FLOOR) return fail(SF_ERR_INVALID_ARGUMENT, "unknown K rule");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (b->precision) {
+    // FP32 top-K vectors (n <= 128 in shared memory, larger in global scratch), then the FP64
+    // refinement and re-projection of the weights, then the e4m3 per-beam scales
+    const int np = (int)b->peig_items.size();
+    if (shrink) return fail(SF_ERR_UNSUPPORTED, "the precision path nulls (no shrink mode)");
+    BT_TRY(sf_launch_eig_topk_vectors(b->d_peig_items, 0, b->eig_small_count, 128, d_vis, b->d_fixed, k_rule, delta,
+                                      d_evals, d_counts, b->d_u, nullptr, 0, b->d_status, s),
+           "precision eig");
+    BT_TRY(sf_launch_eig_topk_vectors(b->d_peig_items, b->eig_small_count, np - b->eig_small_count, b->n_max, d_vis,
+                                      b->d_fixed, k_rule, delta, d_evals, d_counts, b->d_u, b->d_gA, b->gA_grid,
+                                      b->d_status, s),
+           "precision eig (global working matrices)");
+    if (!d_counts) return fail(SF_ERR_INVALID_ARGUMENT, "the precision path needs the counts buffer");
+    BT_TRY(sf_launch_refine64(b->d_peig_items, np, d_vis, b->d_u, d_counts, b->d_weights, b->d_weff, b->B,
+                              b->refine_steps, b->orthogonal, b->d_ritz, b->d_resid, b->d_status, s),
+           "FP64 refinement");
+    if (b->L.beam_op == SF_BEAM_E4M3 || b->L.beam_op == SF_BEAM_E4M3_SPLIT)
+      BT_TRY(sf_batch_launch_scales(b->L, b->n_units, b->d_weff, b->d_scales, s), "beam scales");
+    return SF_OK;
+  }
   auto launch = [&](int g, cudaStream_t st) {
     return sf_launch_eig_topk_items(b->d_eig_items, b->eig_first[g], b->eig_first[g + 1] - b->eig_first[g],
                                     b->eig_nmax[g], b->B, d_vis, nullptr, b->d_weights, b->d_fixed, k_rule, delta,
@@ -394,6 +498,59 @@ int sf_batch_run(sf_batch *b, const int8_t *d_samples, int32_t k_rule, float del
   if (int rc = sf_batch_correlate(b, d_samples, d_vis, stream)) return rc;
   if (int rc = sf_batch_covariance_eig(b, d_vis, k_rule, delta, shrink, d_evals, d_counts, stream)) return rc;
   return sf_batch_beamform(b, d_samples, d_beams_f16, stream);
+}
+
+int sf_batch_set_precision(sf_batch *b, int32_t beam_precision, int32_t refine_steps, int32_t orthogonal) {
+  if (int rc = check(b)) return rc;
+  if (beam_precision < SF_BEAM_FP16 || beam_precision > SF_BEAM_E4M3_SPLIT)
+    return fail(SF_ERR_INVALID_ARGUMENT, "unknown beam precision %d", beam_precision);
+  if (refine_steps < -1 || refine_steps > 8) return fail(SF_ERR_INVALID_ARGUMENT, "refine_steps outside [-1, 8]");
+  if (refine_steps < 0 && b->needs_precision)
+    return fail(SF_ERR_UNSUPPORTED, "more than 128 receivers or 16 beams need the FP64-refined path");
+  if ((beam_precision == SF_BEAM_E4M3 || beam_precision == SF_BEAM_E4M3_SPLIT) && refine_steps < 0)
+    return fail(SF_ERR_UNSUPPORTED, "e4m3 beams need the FP64-refined path (it computes the per-beam scales)");
+  b->L.beam_op = beam_precision;
+  b->precision = refine_steps >= 0;
+  b->refine_steps = refine_steps < 0 ? 0 : refine_steps;
+  b->orthogonal = orthogonal ? 1 : 0;
+  // e4m3 atoms pair the int8 boxes: an even number per slab
+  if ((beam_precision == SF_BEAM_E4M3 || beam_precision == SF_BEAM_E4M3_SPLIT) && (b->L.beam_sa & 1)) {
+    b->L.beam_sa = 2;
+    if (int rc = schedule(b)) return rc;
+  }
+  return SF_OK;
+}
+
+int sf_batch_effective_weights(sf_batch *b, float *d_weff, void *stream) {
+  if (int rc = check(b)) return rc;
+  if (!d_weff) return fail(SF_ERR_INVALID_ARGUMENT, "weff is NULL");
+  BT_TRY(cudaMemcpyAsync(d_weff, b->d_weff, sizeof(float2) * b->weff_elems, cudaMemcpyDeviceToDevice,
+                         static_cast<cudaStream_t>(stream)),
+         "effective weights copy");
+  return SF_OK;
+}
+
+int sf_batch_precision_report(sf_batch *b, float *h_residuals, double *h_ritz, void *stream) {
+  if (int rc = check(b)) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t np = b->peig_items.size();
+  // host copies are [unit][Pol] ordered: map from the precision item order
+  std::vector<float> r(np * 2);
+  std::vector<double> t(np * sf_refine64_kmax());
+  BT_TRY(cudaMemcpyAsync(r.data(), b->d_resid, sizeof(float) * r.size(), cudaMemcpyDeviceToHost, s), "report");
+  BT_TRY(cudaMemcpyAsync(t.data(), b->d_ritz, sizeof(double) * t.size(), cudaMemcpyDeviceToHost, s), "report");
+  BT_TRY(cudaStreamSynchronize(s), "report");
+  const int km = sf_refine64_kmax();
+  for (size_t i = 0; i < np; ++i) {
+    const int idx = b->peig_items[i].count_idx;
+    if (h_residuals) {
+      h_residuals[2 * idx] = r[2 * i];
+      h_residuals[2 * idx + 1] = r[2 * i + 1];
+    }
+    if (h_ritz)
+      for (int k = 0; k < km; ++k) h_ritz[(size_t)idx * km + k] = t[i * km + k];
+  }
+  return SF_OK;
 }
 
 int sf_batch_status(sf_batch *b, void *stream, uint32_t *out_bits) {

@@ -22,6 +22,7 @@
 //      P = I - sum_k w_k u_k u_k^H (null: w = 1 on the un-whitened u;
 //      shrink: w = 1 - lambda_bar / lambda_k on the whitened v).
 #include <cstdio>
+#include <cstring>
 
 #include "sf_common.cuh"
 #include "sf_plan.cuh"
@@ -29,7 +30,8 @@
 namespace {
 
 constexpr int NT_PLAN = 128;  // threads per matrix on the plan path (six CTAs per SM)
-constexpr int MAX_N = 128;
+constexpr int MAX_N = 128;   // shared-memory working matrix
+constexpr int MAX_N_GLOBAL = 256;  // working matrix in global scratch
 constexpr int GROUP = 8;  // inverse-iteration vectors solved at once (one lane of warp 0 each)
 constexpr int INV_ITERS = 3;
 constexpr int MAX_B = 16;  // beams per pol handled by the projection step
@@ -55,15 +57,27 @@ struct TopkArgs {
   // walked grid-stride; NULL otherwise.
   const int32_t *list;
   const int32_t *list_count;
+  // matrices of the launch when CTAs walk them grid-stride (0: one per CTA)
+  int n_items;
+  // Large matrices: the n x (n+1) working matrix lives in this global scratch
+  // (one region of a_ld floats2 per CTA) instead of shared memory.
+  float2 *gA;
+  long long a_ld;
+  // Vectors out: the top-K un-whitened, normalised eigenvectors are written
+  // to u_out + (item u_off, or matrix x xk x n) + k n instead of projecting
+  // weights (B = 0).
+  float2 *u_out;
 };
 
 // rows of the eigenvector workspace X for an n x n matrix
 __host__ __device__ inline int topk_xk(int n) { return n < MAX_XK ? n : MAX_XK; }
 
-__host__ __device__ inline size_t topk_floats(int n, int B, int NW) {
-  // float2: A (n x (n+1)), 2 v, p, tau, Z (NW x n), Wp (B x n), W0 (B x n), coef (NW x B)
+__host__ __device__ inline size_t topk_floats(int n, int B, int NW, bool a_in_smem = true) {
+  // float2: A (n x (n+1), unless in global scratch), 2 v, p, tau, Z (NW x n), Wp (B x n), W0 (B x n),
+  //         coef (NW x B)
   // float:  X (xk x n), LU workspace (5 GROUP x n), d, e, e2, lam, sd
-  const size_t f2 = (size_t)n * (n + 1) + 4 * (size_t)n + (size_t)NW * n + 2 * (size_t)B * n + (size_t)NW * B;
+  const size_t f2 = (a_in_smem ? (size_t)n * (n + 1) : 0) + 4 * (size_t)n + (size_t)NW * n + 2 * (size_t)B * n +
+                    (size_t)NW * B;
   const size_t f = (size_t)topk_xk(n) * n + 5 * (size_t)GROUP * n + 5 * (size_t)n;
   return ((2 * f2 + f) + 3) & ~(size_t)3;
 }
@@ -177,12 +191,13 @@ __global__ void __launch_bounds__(NTT, NTT <= 128 ? (NPL <= 2 ? 6 : 1) : 1) sf_e
   const int warp = tid >> 5;
   const int lane = tid & 31;
   const int B = a.B;
-  const int count = a.list ? *a.list_count : static_cast<int>(gridDim.x);
+  const int count = a.list ? *a.list_count : (a.n_items > 0 ? a.n_items : static_cast<int>(gridDim.x));
   for (int mi = blockIdx.x; mi < count; mi += gridDim.x) {
   if (mi != static_cast<int>(blockIdx.x)) __syncthreads();  // the previous matrix's shared memory is free
   // this matrix: size, packed upper triangle (baseline (i,j) at entry baseline_of(i,j), each entry
   // [Pol][Pol][2] int32), receiver factors, weights [B][n], outputs
   int n, pol, fixedK;
+  long long uoff;
   const int32_t *visb;
   const float2 *dp;
   const __half2 *w;
@@ -196,7 +211,8 @@ __global__ void __launch_bounds__(NTT, NTT <= 128 ? (NPL <= 2 ? 6 : 1) : 1) sf_e
     visb = a.vis + it.vis_off;
     dp = a.factors ? a.factors + it.factor_off : nullptr;
     w = a.weights + it.weight_off;
-    we = a.weff + it.weff_off;
+    we = a.weff ? a.weff + it.weff_off : nullptr;
+    uoff = it.u_off;
     ev_out = a.evals ? a.evals + it.eval_off : nullptr;
     cnt_out = a.counts ? a.counts + it.count_idx : nullptr;
     fixedK = a.fixed_counts ? a.fixed_counts[it.count_idx] : 0;
@@ -208,7 +224,8 @@ __global__ void __launch_bounds__(NTT, NTT <= 128 ? (NPL <= 2 ? 6 : 1) : 1) sf_e
     visb = a.vis + (size_t)c * a.NBL * 8;
     dp = a.factors + (size_t)bt * n;
     w = a.weights + (size_t)bt * B * n;
-    we = a.weff + (size_t)bt * 2 * B * n;
+    we = a.weff ? a.weff + (size_t)bt * 2 * B * n : nullptr;
+    uoff = (long long)bt * topk_xk(n) * n;
     ev_out = a.evals ? a.evals + (size_t)bt * n : nullptr;
     cnt_out = a.counts ? a.counts + bt : nullptr;
     fixedK = a.fixed_counts ? a.fixed_counts[c] : 0;
@@ -216,8 +233,8 @@ __global__ void __launch_bounds__(NTT, NTT <= 128 ? (NPL <= 2 ? 6 : 1) : 1) sf_e
   const int ld = n + 1;
   const int xk = topk_xk(n);
 
-  float2 *A = reinterpret_cast<float2 *>(smem);  // n x ld
-  float2 *vbuf = A + n * ld;                     // reflectors k (even / odd k)
+  float2 *A = a.gA ? a.gA + (size_t)blockIdx.x * a.a_ld : reinterpret_cast<float2 *>(smem);  // n x ld
+  float2 *vbuf = a.gA ? reinterpret_cast<float2 *>(smem) : A + n * ld;  // reflectors k (even / odd k)
   float2 *pb = vbuf + 2 * n;                     // tau A v
   float2 *taus = pb + n;                         // reflector scalars
   float2 *Z = taus + n;                          // NW back-transformed vectors
@@ -712,7 +729,10 @@ __global__ void __launch_bounds__(NTT, NTT <= 128 ? (NPL <= 2 ? 6 : 1) : 1) sf_e
       }
 #pragma unroll
       for (int t = 0; t < NPL; ++t)
-        if (lane + 32 * t < n) z[lane + 32 * t] = zz[t];
+        if (lane + 32 * t < n) {
+          z[lane + 32 * t] = zz[t];
+          if (a.u_out) a.u_out[uoff + (long long)r * n + lane + 32 * t] = zz[t];
+        }
       // c_m = wgt (W_m . z) against the original weights: all partial sums
       // first, then the reductions
       {
@@ -755,11 +775,12 @@ __global__ void __launch_bounds__(NTT, NTT <= 128 ? (NPL <= 2 ? 6 : 1) : 1) sf_e
     }
     __syncthreads();
   }
-  for (int e0 = tid; e0 < B * n; e0 += NT) {
-    const int col = e0 - (e0 / n) * n;
-    we[e0] = cmul(W0[e0], factor(col));
-    we[B * n + e0] = cmul(Wp[e0], factor(col));
-  }
+  if (we)
+    for (int e0 = tid; e0 < B * n; e0 += NT) {
+      const int col = e0 - (e0 / n) * n;
+      we[e0] = cmul(W0[e0], factor(col));
+      we[B * n + e0] = cmul(Wp[e0], factor(col));
+    }
   }  // matrices of this CTA
 }
 
@@ -807,6 +828,10 @@ cudaError_t sf_launch_eig_topk_items(const SfEigItem *items, int first, int coun
   a.first_item = first;
   a.list = nullptr;
   a.list_count = nullptr;
+  a.n_items = 0;
+  a.gA = nullptr;
+  a.a_ld = 0;
+  a.u_out = nullptr;
   // large matrices take more threads: the rank-2 update is spread over all warps but one
   cudaError_t e;
   if (n_max <= 32) {
@@ -850,6 +875,10 @@ cudaError_t sf_launch_eig_topk(const sf_plan *p, const int32_t *vis, int k_rule,
   a.first_item = 0;
   a.list = nullptr;
   a.list_count = nullptr;
+  a.n_items = 0;
+  a.gA = nullptr;
+  a.a_ld = 0;
+  a.u_out = nullptr;
   const size_t smem = sf_eig_topk_smem(p->R, p->B);
   cudaError_t e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<2, NT_PLAN>), smem);
   if (e != cudaSuccess) return e;
@@ -881,10 +910,58 @@ cudaError_t sf_launch_eig_topk_list(const sf_plan *p, const int32_t *vis, const 
   a.first_item = 0;
   a.list = list;
   a.list_count = list_count;
+  a.n_items = 0;
+  a.gA = nullptr;
+  a.a_ld = 0;
+  a.u_out = nullptr;
   const size_t smem = sf_eig_topk_smem(p->R, p->B);
   cudaError_t e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<2, NT_PLAN>), smem);
   if (e != cudaSuccess) return e;
   const int grid = max_count < 6 * p->num_sms ? max_count : 6 * p->num_sms;
   sf_eig_topk_kernel<2, NT_PLAN><<<grid, NT_PLAN, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
+// Eigenvectors out, for matrices of up to 256 receivers (the working matrix in
+// global scratch above 128): per item the top-K un-whitened normalised
+// eigenvectors at u_out + item.u_off, K at counts, eigenvalues at evals;
+// no weight projection.  scratch holds min(count, grid) x n_max x (n_max + 1)
+// float2; returns the grid used (<= max_grid).
+cudaError_t sf_launch_eig_topk_vectors(const SfEigItem *items, int first, int count, int n_max, const int32_t *vis,
+                                       const int32_t *fixed_counts, int k_rule, float delta, float *evals,
+                                       int32_t *counts, float2 *u_out, float2 *scratch, int max_grid,
+                                       uint32_t *status, cudaStream_t stream) {
+  if (count <= 0) return cudaSuccess;
+  if (n_max > MAX_N_GLOBAL) return cudaErrorInvalidValue;
+  TopkArgs a;
+  memset(&a, 0, sizeof(a));
+  a.vis = vis;
+  a.fixed_counts = fixed_counts;
+  a.evals = evals;
+  a.counts = counts;
+  a.status = status;
+  a.R = n_max;
+  a.B = 0;
+  a.k_rule = k_rule;
+  a.delta = delta;
+  a.items = items;
+  a.first_item = first;
+  a.u_out = u_out;
+  cudaError_t e;
+  if (n_max <= 128) {
+    const size_t smem = topk_floats(n_max, 0, 16) * sizeof(float);
+    e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<4, 512>), smem);
+    if (e != cudaSuccess) return e;
+    sf_eig_topk_kernel<4, 512><<<count, 512, smem, stream>>>(a);
+  } else {
+    const int grid = count < max_grid ? count : max_grid;
+    a.gA = scratch;
+    a.a_ld = (long long)n_max * (n_max + 1);
+    a.n_items = count;
+    const size_t smem = topk_floats(n_max, 0, 16, false) * sizeof(float);
+    e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_topk_kernel<8, 512>), smem);
+    if (e != cudaSuccess) return e;
+    sf_eig_topk_kernel<8, 512><<<grid, 512, smem, stream>>>(a);
+  }
   return cudaGetLastError();
 }

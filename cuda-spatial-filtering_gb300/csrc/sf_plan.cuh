@@ -92,6 +92,7 @@ int sf_eig_supported(const sf_plan *p, char *why, size_t why_len);
 // weff_off ([2B][n] float2), eigenvalues at eval_off ([n]), K at count_idx.
 struct SfEigItem {
   long long vis_off, factor_off, weight_off, weff_off, eval_off;
+  long long u_off;  // eigenvectors-out form: float2 offset of this matrix's top-K vectors [K][n]
   int n, pol, count_idx, unit;
 };
 
@@ -103,6 +104,10 @@ int sf_eig_topk_max_b();
 cudaError_t sf_launch_eig_topk_list(const sf_plan *p, const int32_t *vis, const int32_t *list, const int32_t *list_count,
                                     int max_count, int k_rule, float delta, int shrink, float *evals, int32_t *counts,
                                     cudaStream_t stream);
+cudaError_t sf_launch_eig_topk_vectors(const SfEigItem *items, int first, int count, int n_max, const int32_t *vis,
+                                       const int32_t *fixed_counts, int k_rule, float delta, float *evals,
+                                       int32_t *counts, float2 *u_out, float2 *scratch, int max_grid,
+                                       uint32_t *status, cudaStream_t stream);
 cudaError_t sf_launch_eig_topk_items(const SfEigItem *items, int first, int count, int n_max, int B,
                                      const int32_t *vis, const float2 *factors, const __half2 *weights,
                                      const int32_t *fixed_counts, int k_rule, float delta, int shrink, float *evals,

@@ -77,7 +77,7 @@ __global__ void sf_proposer_features_kernel(const int32_t *vis, int R, int NBL, 
   __shared__ float s[RR_MAX_N * 2];
   const int32_t *vb = vis + (size_t)c * NBL * 8;
   for (int i = threadIdx.x; i < R; i += blockDim.x)
-    s[i] = rsqrtf(fmaxf(static_cast<float>(vb[((size_t)baseline_of(i, i) * 2 + p) * 4]), 1e-10f));
+    s[i] = rsqrtf(fmaxf(static_cast<float>(vb[((size_t)baseline_of(i, i) * 2 + p) * 4 + p * 2]), 1e-10f));
   __syncthreads();
   const float inv_n = 1.0f / static_cast<float>(R);
   __nv_bfloat16 *xr = x + (size_t)row * ldx;

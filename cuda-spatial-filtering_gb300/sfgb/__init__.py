@@ -31,6 +31,10 @@ SF_EIG_SAME_POL_WHITENED = 1
 SF_K_FIXED = 0
 SF_K_DETECT = 1
 SF_K_NOISE_FLOOR = 2
+SF_BEAM_FP16 = 0
+SF_BEAM_BF16 = 1
+SF_BEAM_E4M3 = 2
+SF_BEAM_E4M3_SPLIT = 3
 # device status bits (sf_device_bits)
 SF_DEV_TIMEOUT_TMA = 1 << 0
 SF_DEV_TIMEOUT_CONVERT = 1 << 1
@@ -92,6 +96,9 @@ _SIGS = {
     "sf_batch_beamform": ([_P, _P, _P, _P], ctypes.c_int),
     "sf_batch_run": ([_P, _P, _I32, ctypes.c_float, _I32, _P, _P, _P, _P, _P], ctypes.c_int),
     "sf_batch_status": ([_P, _P, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
+    "sf_batch_set_precision": ([_P, _I32, _I32, _I32], ctypes.c_int),
+    "sf_batch_precision_report": ([_P, _P, _P, _P], ctypes.c_int),
+    "sf_batch_effective_weights": ([_P, _P, _P], ctypes.c_int),
     "sf_batch_autotune": ([_P, _P, _I32, ctypes.c_float, _P, _P, _P, _P, _P, ctypes.c_char_p, _I32], ctypes.c_int),
     "sf_proposer_create": ([_I32, _I32, _I32, ctypes.POINTER(_P)], ctypes.c_int),
     "sf_proposer_destroy": ([_P], ctypes.c_int),
@@ -452,6 +459,30 @@ class Batch:
         bits = ctypes.c_uint32(0)
         rc = lib().sf_batch_status(self._h, _stream(stream), ctypes.byref(bits))
         return rc, bits.value
+
+    def set_precision(self, beam_precision, refine_steps=2, orthogonal=True):
+        _check(lib().sf_batch_set_precision(self._h, int(beam_precision), int(refine_steps), int(bool(orthogonal))))
+
+    def effective_weights(self, stream=None):
+        """Per unit complex128 [Pol][2B][R] effective weights of the last eigen stage."""
+        import torch
+        w = torch.empty(4 * self.totals["weights"], dtype=torch.float32, device="cuda")
+        _check(lib().sf_batch_effective_weights(self._h, _ptr(w), _stream(stream)))
+        torch.cuda.synchronize()
+        h = w.cpu().numpy().astype(np.float64)
+        out = []
+        for u, R in enumerate(self.receivers):
+            o = 4 * int(self.layout["weights"][u])
+            blk = h[o:o + 2 * 2 * self.B * int(R) * 2].reshape(2, 2 * self.B, int(R), 2)
+            out.append(blk[..., 0] + 1j * blk[..., 1])
+        return out
+
+    def precision_report(self, stream=None):
+        """(residuals [u][Pol][2] before/after, FP64 Ritz values [u][Pol][8]) of the last refined run."""
+        r = np.zeros((self.n_units, 2, 2), np.float32)
+        t = np.zeros((self.n_units, 2, 8), np.float64)
+        _check(lib().sf_batch_precision_report(self._h, r.ctypes.data_as(_P), t.ctypes.data_as(_P), _stream(stream)))
+        return r, t
 
     def autotune(self, samples, k_rule, delta, vis, evals, counts, beams, stream=None):
         """Runs the autotuner; returns its JSON record (dict)."""

@@ -266,7 +266,8 @@ int sf_run_adaptive(sf_plan *plan, const int8_t *d_samples, const int16_t *d_sca
 /* ---- batched sub-arrays of uneven size --------------------------------------- */
 
 /* A batch of units: one channel-integration each of a sub-array with its own receiver count
- * (a multiple of 4, at most 128), all with n_samples (a multiple of 128) samples and n_beams beams.
+ * (a multiple of 4, at most 256; above 128 the refined precision path), all with n_samples (a
+ * multiple of 128) samples and n_beams beams (at most 64; above 16 the refined path).
  * The whole mixed batch runs through one persistent tcgen05 correlator launch, the eigensolver
  * (one launch per size class, side by side on forked streams) and one persistent tcgen05
  * beamformer launch over a shared work list -- all capturable into one CUDA graph.  No counterpart
@@ -283,6 +284,14 @@ int sf_run_adaptive(sf_plan *plan, const int8_t *d_samples, const int16_t *d_sca
  *   evals    float [Pol][R] at eval_off[u] (whitened, ascending);  counts int32 [u][Pol]
  *   beams    fp16  [Pol][2B][T][2] at beam_off[u] (fp16 pairs; slot 0 original, slot 1 projected)
  * totals[5] = {sample bytes, vis elements, weight pairs, eval elements, beam pairs}. */
+/* Beam operand precision of the batched beamformer (sf_batch_set_precision); accumulation is FP32. */
+typedef enum sf_beam_precision {
+  SF_BEAM_FP16 = 0,       /* fp16 samples (exact) and weights: the plain path */
+  SF_BEAM_BF16 = 1,       /* bf16 samples (exact) and weights */
+  SF_BEAM_E4M3 = 2,       /* e4m3 samples (rounded) and weights with per-beam scales (kind::f8f6f4) */
+  SF_BEAM_E4M3_SPLIT = 3  /* e4m3 weights with per-beam scales, samples exact as 16 (x >> 4) + (x & 15) */
+} sf_beam_precision;
+
 typedef struct sf_batch sf_batch;
 int sf_batch_create(int32_t n_units, const int32_t *h_receivers, int32_t n_samples, int32_t n_beams,
                     sf_batch **out_batch);
@@ -302,6 +311,25 @@ int sf_batch_run(sf_batch *batch, const int8_t *d_samples, int32_t k_rule, float
                  int32_t *d_vis, float *d_evals, int32_t *d_counts, uint16_t *d_beams_f16, void *stream);
 /* Reads and clears the batch's device error bits; synchronises `stream`. */
 int sf_batch_status(sf_batch *batch, void *stream, uint32_t *out_bits);
+/* The precision form: beam operands in `beam_precision` (sf_beam_precision), and -- with
+ * refine_steps >= 0 -- the eigensolver's FP32 top-K vectors refined in FP64 (refine_steps subspace
+ * steps, each A V, orthonormalisation and a Rayleigh-Ritz solve of V^H A V) before the weights are
+ * projected in FP64, onto the orthogonal complement of an orthonormalised nulled subspace
+ * (orthogonal != 0) or with the reference's I - U U^H of the un-whitened vectors (orthogonal = 0).
+ * refine_steps = -1 keeps the FP32 top-K path (at most 128 receivers and 16 beams).  Units of more
+ * than 128 receivers or batches of more than 16 beams always take the refined path; e4m3 beams need
+ * it (it computes their per-beam scales: s = max |re w|, |im w| / 448, weights / s in e4m3, output
+ * times s).  No counterpart in the reference (FP32 cuSOLVER vectors, fp16 projector and beams,
+ * lambda_adaptive_beamformed_spectra_pipeline.hpp:679-798). */
+int sf_batch_set_precision(sf_batch *batch, int32_t beam_precision, int32_t refine_steps, int32_t orthogonal);
+/* The effective weights of the last eigen stage (what the beamformer applies), float pairs per unit
+ * [Pol][2B][R][2] (slot 0 original, slot 1 projected) at weight_off[u] x 4 floats (the layout's weight
+ * offsets, doubled for the two slots).  Asynchronous device-to-device copy. */
+int sf_batch_effective_weights(sf_batch *batch, float *d_weff, void *stream);
+/* After a refined run: per (unit, pol) the relative residual max_k ||A v_k - theta_k v_k|| / theta_max of
+ * the FP32 vectors and of the refined ones (h_residuals [u][Pol][2], may be NULL) and the FP64 Ritz
+ * values (h_ritz [u][Pol][8], descending, 0 past K; may be NULL).  Synchronises `stream`. */
+int sf_batch_precision_report(sf_batch *batch, float *h_residuals, double *h_ritz, void *stream);
 /* Times candidate work-list packings, ring depths and eigensolver concurrency on the given buffers
  * (CUDA events on `stream`, which it synchronises: call it at set-up, outside any capture), keeps
  * the fastest for later calls and writes a JSON record of every candidate and the choice into

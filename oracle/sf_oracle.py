@@ -680,12 +680,14 @@ def unit_samples_split(x):
     return re, im
 
 
-def unit_chain(x, weights, k_rule="fixed", k_fixed=0, delta=10.0):
+def unit_chain(x, weights, k_rule="fixed", k_fixed=0, delta=10.0, orthogonal=False, beam_samples=None):
     """The adaptive chain of one unit.  weights fp16 pairs [Pol][B][R][2].
     k_rule: "fixed" (k_fixed, an int or a per-pol pair), "noise" (K =
-    #{lambda > delta x median}) or "detect" (detect_k_f32).  Returns vis (int64
-    [NBL][Pol][Pol][2]), evals [Pol][R] (whitened, LAPACK), counts [Pol],
-    w_eff [Pol][2B][R] and beams [Pol][2B][T] (complex)."""
+    #{lambda > delta x median}) or "detect" (detect_k_f32).  orthogonal: null
+    with the orthogonal projector onto the complement of span(U) (U = the
+    un-whitened top-K vectors, orthonormalised) instead of I - U U^H.
+    Returns vis (int64 [NBL][Pol][Pol][2]), evals [Pol][R] (whitened, LAPACK),
+    counts [Pol], w_eff [Pol][2B][R] and beams [Pol][2B][T] (complex)."""
     T, R = x.shape[0], x.shape[1]
     sh = Shape(1, 1, T, R, R, 1, 1)
     re, im = unit_samples_split(x)
@@ -710,12 +712,17 @@ def unit_chain(x, weights, k_rule="fixed", k_fixed=0, delta=10.0):
             k = int(kf[p] if kf.size > 1 else kf[0])
         k = max(0, min(R, k))
         u = unwhiten_normalize(v, s)
-        pm = null_projection(u, k)
+        if orthogonal and k > 0:
+            q, _ = np.linalg.qr(u[:, R - k:])
+            pm = np.eye(R, dtype=np.complex128) - q @ np.conj(q.T)
+        else:
+            pm = null_projection(u, k)
         evals[p] = lam
         counts[p] = k
         w_eff[p, :B] = wc[p]
         w_eff[p, B:] = wc[p] @ pm
-    beams = np.einsum("pmr,prt->pmt", w_eff, re[0] + 1j * im[0])
+    ts = T if beam_samples is None else int(beam_samples)  # beams of the first ts samples
+    beams = np.einsum("pmr,prt->pmt", w_eff, re[0][..., :ts] + 1j * im[0][..., :ts])
     return {"vis": vis[0], "evals": evals, "counts": counts, "w_eff": w_eff, "beams": beams}
 
 
