@@ -216,6 +216,14 @@ int sf_batch_create(int32_t n_units, const int32_t *h_receivers, int32_t n_sampl
   b->eval_off.resize(n_units);
   b->beam_off.resize(n_units);
   int max_atoms = 0;
+  for (int u = 0; u < n_units; ++u) max_atoms = std::max(max_atoms, (4 * b->R[u] + 63) / 64);
+  // beams per beamformer item: the most whose fp16 weight tile (all the unit's atoms x
+  // 4 x beams rows of 128 B) fits beside two rings of two slabs
+  int nbg = std::min(2 * n_beams, MAX_NBG);
+  while (nbg > 4 && sf_batch_smem_bytes(true, 2, 2, 2, static_cast<uint32_t>(max_atoms * (((4 * nbg + 15) / 16) * 16) * 128)) >
+                        (size_t)sf_device_max_smem())
+    nbg >>= 1;
+  max_atoms = 0;
   for (int u = 0; u < n_units; ++u) {
     const int R = b->R[u], c = cls_of[R];
     SfBatchUnit &un = b->units[u];
@@ -239,7 +247,6 @@ int sf_batch_create(int32_t n_units, const int32_t *h_receivers, int32_t n_sampl
     sf_batch_corr_items(u, R, b->corr_items);
     // beamformer items: groups of at most MAX_NBG beams (all slots) per pol
     const int NB = 2 * n_beams;
-    const int nbg = std::min(NB, MAX_NBG);
     for (int g0 = 0; g0 < NB; g0 += nbg) {
       SfBatchItem bi{};
       bi.unit = u;
@@ -251,7 +258,7 @@ int sf_batch_create(int32_t n_units, const int32_t *h_receivers, int32_t n_sampl
     }
     b->n_max = std::max(b->n_max, R);
   }
-  b->L.NBG = std::min(2 * n_beams, MAX_NBG);
+  b->L.NBG = nbg;
   b->L.beam_op = SF_BEAM_FP16;
   b->needs_precision = b->n_max > sf_eig_topk_max_n() || n_beams > sf_eig_topk_max_b();
   b->precision = b->needs_precision;
@@ -325,9 +332,14 @@ int sf_batch_create(int32_t n_units, const int32_t *h_receivers, int32_t n_sampl
   b->L.beam_grid = sms;
   b->L.corr_ni = 2;
   b->L.corr_nf = 2;
-  b->L.beam_sa = 2;
-  b->L.beam_ni = 3;
-  b->L.beam_nf = 3;
+  // deepest beamformer rings that fit beside the weight tile
+  {
+    const uint32_t wt = static_cast<uint32_t>(max_atoms * (((4 * nbg + 15) / 16) * 16) * 128);
+    const int depth = sf_batch_smem_bytes(true, 2, 3, 3, wt) <= (size_t)sf_device_max_smem() ? 3 : 2;
+    b->L.beam_sa = 2;
+    b->L.beam_ni = depth;
+    b->L.beam_nf = depth;
+  }
 
   int rc = upload(&b->d_units, b->units);
   if (!rc) rc = upload(&b->d_corr_items, b->corr_items);

@@ -308,30 +308,54 @@ __global__ void sf_proposer_targets_kernel(const int32_t *vis, const float *eval
   }
 }
 
-// Weighted squared error and its gradient: dY = 2 w (Y - T) / rows (bf16),
-// loss += sum w (Y - T)^2 / rows; output j of a row belongs to vector j / (2R).
+// Phase-invariant distance of each proposed vector y_k to its target t_k
+// (|t_k| = 1): min over phi of ||y_k - t_k e^{i phi}||^2 = ||y_k||^2 + 1 -
+// 2 |<t_k, y_k>|, weighted by w_k; gradient 2 w_k (y_k - t_k e^{i psi}) / rows
+// with psi = arg <t_k, y_k> (a vector is only defined up to its phase, so the
+// loss does not ask for one).  One warp per (row, vector); loss += sum / rows.
 __global__ void sf_proposer_loss_kernel(const float *y, const float *t, const float *tw, int rows, int width, int R,
                                         __nv_bfloat16 *dy, int lddy, float *loss) {
-  const int row = blockIdx.x;
-  float part = 0.0f;
-  for (int j = threadIdx.x; j < lddy; j += blockDim.x) {
-    float g = 0.0f;
-    if (j < width) {
-      const float w = tw[row * 4 + j / (2 * R)];
-      const float d = y[(size_t)row * width + j] - t[(size_t)row * width + j];
-      part += w * d * d;
-      g = 2.0f * w * d / static_cast<float>(rows);
-    }
-    dy[(size_t)row * lddy + j] = __float2bfloat16_rn(g);
-  }
-  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  const int row = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nvec = width / (2 * R);
   __shared__ float red[32];
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
+  float part = 0.0f;
+  for (int k = warp; k < nvec; k += blockDim.x >> 5) {
+    const float *yk = y + (size_t)row * width + k * 2 * R;
+    const float *tk = t + (size_t)row * width + k * 2 * R;
+    float dr = 0.0f, di = 0.0f, yy = 0.0f;  // <t, y> = sum conj(t) y, ||y||^2
+    for (int i = lane; i < R; i += 32) {
+      const float yr = yk[2 * i], yi = yk[2 * i + 1], tr = tk[2 * i], ti = tk[2 * i + 1];
+      dr += tr * yr + ti * yi;
+      di += tr * yi - ti * yr;
+      yy += yr * yr + yi * yi;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      dr += __shfl_xor_sync(0xffffffffu, dr, o);
+      di += __shfl_xor_sync(0xffffffffu, di, o);
+      yy += __shfl_xor_sync(0xffffffffu, yy, o);
+    }
+    const float w = tw[row * 4 + k];
+    const float mag = sqrtf(dr * dr + di * di);
+    const float cr = mag > 0.0f ? dr / mag : 1.0f, ci = mag > 0.0f ? di / mag : 0.0f;  // e^{i psi}
+    if (lane == 0) part += w * (yy + 1.0f - 2.0f * mag);
+    const float g = 2.0f * w / static_cast<float>(rows);
+    __nv_bfloat16 *dk = dy + (size_t)row * lddy + k * 2 * R;
+    for (int i = lane; i < R; i += 32) {
+      const float tr = tk[2 * i], ti = tk[2 * i + 1];
+      // t e^{i psi}
+      const float er = tr * cr - ti * ci, ei = tr * ci + ti * cr;
+      dk[2 * i] = __float2bfloat16_rn(g * (yk[2 * i] - er));
+      dk[2 * i + 1] = __float2bfloat16_rn(g * (yk[2 * i + 1] - ei));
+    }
+  }
+  // padding columns of dY stay zero
+  for (int j = width + threadIdx.x; j < lddy; j += blockDim.x) dy[(size_t)row * lddy + j] = __float2bfloat16_rn(0.0f);
+  if (lane == 0) red[warp] = part;
   __syncthreads();
   if (threadIdx.x == 0) {
-    float s = 0.0f;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
-    atomicAdd(loss, s / static_cast<float>(rows));
+    float s2 = 0.0f;
+    for (int w2 = 0; w2 < (int)(blockDim.x >> 5); ++w2) s2 += red[w2];
+    atomicAdd(loss, s2 / static_cast<float>(rows));
   }
 }
 
@@ -413,7 +437,7 @@ cudaError_t sf_launch_proposer_targets(const int32_t *vis, const float *evals, c
 cudaError_t sf_launch_proposer_loss(const float *y, const float *t, const float *tw, int rows, int width, int R,
                                     void *dy, int lddy, float *loss, cudaStream_t stream) {
   sf_proposer_loss_kernel<<<rows, 128, 0, stream>>>(y, t, tw, rows, width, R, static_cast<__nv_bfloat16 *>(dy), lddy,
-                                                    loss);
+                                                    loss);  // four warps: one per proposed vector
   return cudaGetLastError();
 }
 

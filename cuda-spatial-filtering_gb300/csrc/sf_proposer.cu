@@ -752,7 +752,10 @@ int sf_covariance_eig_learned(sf_plan *plan, sf_proposer *q, const int32_t *d_vi
   sf_rr_kernel<<<(rows + wpc - 1) / wpc, 32 * wpc, smem, s>>>(a);
   PR_TRY(cudaGetLastError(), "RR launch");
   // the rejected matrices through the full top-K eigensolver
-  PR_TRY(sf_launch_eig_topk_list(plan, d_vis, q->fb_list, q->fb_count, rows, k_rule, delta, 0, nullptr, counts, s),
+  // (with every eigenvalue, as the plain chain computes them: a rejected matrix gets exactly the
+  // plain chain's weights)
+  PR_TRY(sf_launch_eig_topk_list(plan, d_vis, q->fb_list, q->fb_count, rows, k_rule, delta, 0, plan->d_evals, counts,
+                                 s),
          "fallback eig");
   if (d_fallback_count)
     PR_TRY(cudaMemcpyAsync(d_fallback_count, q->fb_count, sizeof(int32_t), cudaMemcpyDeviceToDevice, s),
