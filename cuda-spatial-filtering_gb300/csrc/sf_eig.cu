@@ -392,11 +392,15 @@ cudaError_t sf_launch_eig(const sf_plan *p, const int32_t *vis, int eig_mode, in
                           float delta, int shrink, float *evals, float2 *evecs, int32_t *counts,
                           __half2 *proj, cudaStream_t stream) {
   // The adaptive path needs only eigenvalues and the top-K eigenvectors:
-  // the warp-per-matrix tridiagonal solver (sf_eig_topk.cu) serves it unless
-  // every eigenvector (or the projector itself) is asked for.
-  if (eig_mode == SF_EIG_SAME_POL_WHITENED && evecs == nullptr && proj == nullptr &&
-      sf_eig_topk_supported(p))
-    return sf_launch_eig_topk(p, vis, k_rule, delta, shrink, evals, counts, stream);
+  // the tridiagonal solvers serve it unless every eigenvector (or the
+  // projector itself) is asked for -- sf_eig_small.cu up to 64 receivers and
+  // 16 beams, else sf_eig_topk.cu.
+  if (eig_mode == SF_EIG_SAME_POL_WHITENED && evecs == nullptr && proj == nullptr) {
+    if (sf_eig_small_supported(p))
+      return sf_launch_eig_small(p, vis, k_rule, delta, shrink, evals, counts, nullptr, nullptr, stream);
+    if (sf_eig_topk_supported(p))
+      return sf_launch_eig_topk(p, vis, k_rule, delta, shrink, evals, counts, stream);
+  }
   EigArgs a;
   a.vis = vis;
   a.factors = p->d_factors;

@@ -113,6 +113,13 @@ cudaError_t sf_launch_eig_topk_items(const SfEigItem *items, int first, int coun
                                      const int32_t *fixed_counts, int k_rule, float delta, int shrink, float *evals,
                                      int32_t *counts, float2 *weff, uint32_t *status, cudaStream_t stream);
 int sf_eig_topk_supported(const sf_plan *p);
+// One CTA of four warps per (channel, pol) covariance (sf_eig_small.cu):
+// the adaptive path for R <= 64 and B <= 16.  With list != NULL only the
+// matrices list[0 .. *list_count) (count read on the device, at most 2C).
+int sf_eig_small_supported(const sf_plan *p);
+cudaError_t sf_launch_eig_small(const sf_plan *p, const int32_t *vis, int k_rule, float delta, int shrink,
+                                float *evals, int32_t *counts, const int32_t *list, const int32_t *list_count,
+                                cudaStream_t stream);
 cudaError_t sf_launch_eig_topk(const sf_plan *p, const int32_t *vis, int k_rule, float delta, int shrink,
                                float *evals, int32_t *counts, cudaStream_t stream);
 

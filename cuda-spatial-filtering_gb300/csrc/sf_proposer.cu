@@ -754,9 +754,13 @@ int sf_covariance_eig_learned(sf_plan *plan, sf_proposer *q, const int32_t *d_vi
   // the rejected matrices through the full top-K eigensolver
   // (with every eigenvalue, as the plain chain computes them: a rejected matrix gets exactly the
   // plain chain's weights)
-  PR_TRY(sf_launch_eig_topk_list(plan, d_vis, q->fb_list, q->fb_count, rows, k_rule, delta, 0, plan->d_evals, counts,
-                                 s),
-         "fallback eig");
+  if (sf_eig_small_supported(plan))
+    PR_TRY(sf_launch_eig_small(plan, d_vis, k_rule, delta, 0, plan->d_evals, counts, q->fb_list, q->fb_count, s),
+           "fallback eig");
+  else
+    PR_TRY(sf_launch_eig_topk_list(plan, d_vis, q->fb_list, q->fb_count, rows, k_rule, delta, 0, plan->d_evals,
+                                   counts, s),
+           "fallback eig");
   if (d_fallback_count)
     PR_TRY(cudaMemcpyAsync(d_fallback_count, q->fb_count, sizeof(int32_t), cudaMemcpyDeviceToDevice, s),
            "fallback count");

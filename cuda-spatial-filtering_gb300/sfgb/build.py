@@ -13,7 +13,8 @@ CSRC = ROOT / "csrc"
 BUILD = ROOT / "_build"
 LIB = PKG / "libsfgb.so"
 SOURCES = ["sf_corr.cu", "sf_eig.cu", "sf_eig_topk.cu", "sf_beam.cu", "sf_capi.cu", "sf_noalloc.cu",
-           "sf_spectra.cu", "sf_steering.cu", "sf_batch.cu", "sf_batch_capi.cu", "sf_mlp.cu", "sf_proposer.cu", "sf_refine.cu"]
+           "sf_spectra.cu", "sf_steering.cu", "sf_batch.cu", "sf_batch_capi.cu", "sf_mlp.cu", "sf_proposer.cu", "sf_refine.cu",
+           "sf_eig_small.cu"]
 HEADERS = ["sf_common.cuh", "sf_plan.cuh", "sf_batch.cuh"]
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
