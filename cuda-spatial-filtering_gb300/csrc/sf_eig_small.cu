@@ -710,43 +710,59 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_small_kernel(const SmallEigArgs 
       if (lane + 32 < n) Z[warp * n + lane + 32] = z1;
     }
     __syncthreads();
-    // c_(v,m) = wgt_v (W_m . z_v) for the pass's vectors and every beam
-    for (int idx = tid; idx < rn * B; idx += NT) {
-      const int v = idx / B, mm = idx - v * B;
-      const float2 *wr = W0 + mm * n;
-      const float2 *zv = Z + v * n;
-      float2 acc0 = make_float2(0.0f, 0.0f), acc1 = make_float2(0.0f, 0.0f);
-      int i = 0;
-      for (; i + 1 < n; i += 2) {
-        const float2 t0 = cmul(wr[i], zv[i]), t1 = cmul(wr[i + 1], zv[i + 1]);
-        acc0.x += t0.x;
-        acc0.y += t0.y;
-        acc1.x += t1.x;
-        acc1.y += t1.y;
+    // c_(v,m) = wgt_v (W_m . z_v) for the pass's vectors and every beam: g2 lanes per
+    // (v, m), each summing i = sub (mod g2), reduced by shuffles
+    {
+      const int npair = rn * B;
+      int g2 = 1;
+      while (g2 < 32 && 2 * g2 * npair <= NT) g2 *= 2;
+      for (int pbase = 0; pbase < npair * g2; pbase += NT) {
+        const int pt = (pbase + tid) / g2, sub2 = (pbase + tid) - pt * g2;
+        float2 acc = make_float2(0.0f, 0.0f);
+        if (pt < npair) {
+          const int v = pt / B, mm = pt - v * B;
+          const float2 *wr = W0 + mm * n, *zv = Z + v * n;
+          for (int i = sub2; i < n; i += g2) {
+            const float2 t = cmul(wr[i], zv[i]);
+            acc.x += t.x;
+            acc.y += t.y;
+          }
+        }
+        for (int o = 1; o < g2; o <<= 1) {
+          acc.x += __shfl_xor_sync(FULL, acc.x, o);
+          acc.y += __shfl_xor_sync(FULL, acc.y, o);
+        }
+        if (pt < npair && sub2 == 0) {
+          const int v = pt / B, mm = pt - v * B;
+          float wgt = 1.0f;
+          if (a.shrink) {
+            const float lk = lam[n - 1 - (r0 + v)];
+            wgt = 1.0f - (lk > 0.0f ? lam_bar / lk : 0.0f);
+          }
+          coef[v * SB_MAX + mm] = make_float2(wgt * acc.x, wgt * acc.y);
+        }
       }
-      if (i < n) {
-        const float2 t0 = cmul(wr[i], zv[i]);
-        acc0.x += t0.x;
-        acc0.y += t0.y;
-      }
-      float wgt = 1.0f;
-      if (a.shrink) {
-        const float lk = lam[n - 1 - (r0 + v)];
-        wgt = 1.0f - (lk > 0.0f ? lam_bar / lk : 0.0f);
-      }
-      coef[v * SB_MAX + mm] = make_float2(wgt * (acc0.x + acc1.x), wgt * (acc0.y + acc1.y));
     }
     __syncthreads();
     // Wp_m -= sum_v c_(v,m) conj(z_v)
-    for (int ee = tid; ee < B * n; ee += NT) {
-      const int mm = ee / n, i = ee - mm * n;
-      float2 w = Wp[ee];
-      for (int v = 0; v < rn; ++v) {
-        const float2 t = cmulc(coef[v * SB_MAX + mm], Z[v * n + i]);  // c conj(z_i)
-        w.x -= t.x;
-        w.y -= t.y;
+    {
+      int mm = tid / n, i = tid - (tid / n) * n;  // element ee = mm n + i, advanced by NT
+      const int dm = NT / n, dii = NT - (NT / n) * n;
+      for (int ee = tid; ee < B * n; ee += NT) {
+        float2 w = Wp[ee];
+        for (int v = 0; v < rn; ++v) {
+          const float2 t = cmulc(coef[v * SB_MAX + mm], Z[v * n + i]);  // c conj(z_i)
+          w.x -= t.x;
+          w.y -= t.y;
+        }
+        Wp[ee] = w;
+        i += dii;
+        mm += dm;
+        if (i >= n) {
+          i -= n;
+          ++mm;
+        }
       }
-      Wp[ee] = w;
     }
     __syncthreads();
   }
