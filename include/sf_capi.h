@@ -338,6 +338,70 @@ int sf_batch_autotune(sf_batch *batch, const int8_t *d_samples, int32_t k_rule, 
                       float *d_evals, int32_t *d_counts, uint16_t *d_beams_f16, void *stream, char *report,
                       int32_t report_len);
 
+/* ---- learned subspace proposer -------------------------------------------------- */
+
+/* A 3-layer MLP (in -> hidden -> hidden -> 8 n_receivers; ReLU after the hidden layers) mapping
+ * one (channel, pol) whitened covariance to four complex start vectors of its interference
+ * subspace, trained and run by hand-written BF16 tcgen05 GEMMs (fp32 accumulation, fp32 Adam
+ * master weights).  Its features are the packed upper triangle of the whitened covariance
+ * divided by its trace (2 x baselines real bf16 values, `in`; rows padded to in_ld).  No
+ * counterpart in the reference, whose adaptive pipeline always runs the full eigensolve
+ * (lambda_adaptive_beamformed_spectra_pipeline.hpp:679-686); that solve is the fallback here. */
+typedef struct sf_proposer sf_proposer;
+/* n_receivers in [8, 64]; hidden a multiple of 64; max_rows = the most covariances per call. */
+int sf_proposer_create(int32_t n_receivers, int32_t hidden, int32_t max_rows, sf_proposer **out);
+/* Synchronises the device, then frees. */
+int sf_proposer_destroy(sf_proposer *proposer);
+/* dims[6] = {in, in_ld, hidden, out, out_ld, max_rows}. */
+int sf_proposer_dims(const sf_proposer *proposer, int32_t *dims);
+/* Host fp32 parameters: layer l weight [out_l][in_l] (in_0 = in_ld) and bias [out_l]; resets the
+ * Adam moments; synchronises `stream`.  get_params copies them back (NULL pointers skipped). */
+int sf_proposer_set_params(sf_proposer *proposer, const float *w0, const float *b0, const float *w1,
+                           const float *b1, const float *w2, const float *b2, void *stream);
+int sf_proposer_get_params(const sf_proposer *proposer, float *w0, float *b0, float *w1, float *b1, float *w2,
+                           float *b2, void *stream);
+/* Features of every (channel, pol) covariance of `plan` from its visibilities: bf16 [2C][ldx]
+ * (ldx >= in_ld; row c * 2 + p). */
+int sf_proposer_features(const sf_plan *plan, const int32_t *d_vis, uint16_t *d_x, int32_t ldx, void *stream);
+/* Training targets from a full eigendecomposition (sf_covariance_eig, SF_EIG_SAME_POL_WHITENED, with
+ * eigenvalues and eigenvectors): the top four whitened eigenvectors, largest component real
+ * positive, float [2C][4][R][2], and their weights clamp(1 - median / lambda_k, 0, 1) [2C][4]. */
+int sf_proposer_targets(const sf_plan *plan, const int32_t *d_vis, const float *d_evals, const float *d_evecs,
+                        float *d_targets, float *d_weights, void *stream);
+/* Forward pass: d_y float [rows][out] (vector k of a row at k 2R, re/im interleaved). */
+int sf_proposer_infer(sf_proposer *proposer, const uint16_t *d_x, int32_t rows, float *d_y, void *stream);
+/* One Adam step on a batch: forward, phase-invariant weighted loss
+ * sum_k w_k (|y_k|^2 + 1 - 2 |<t_k, y_k>|) / rows (added to *d_loss), backward, Adam (learning rate lr). */
+int sf_proposer_train_step(sf_proposer *proposer, const uint16_t *d_x, const float *d_targets,
+                           const float *d_weights, int32_t rows, float lr, float *d_loss, void *stream);
+/* Reads and clears the proposer's device error bits; synchronises `stream`. */
+int sf_proposer_status(sf_proposer *proposer, void *stream, uint32_t *out_bits);
+/* The BF16 GEMM behind the proposer, exposed for tests: C[M][N] = sum_k A(m, k) B(n, k), A and B
+ * bf16, K-major ([M][K] / [N][K]) or MN-major ([K][M] / [K][N]); epilogue 0: bf16 relu(acc + bias),
+ * 1: fp32 acc + bias, 2: bf16 acc x [mask > 0], 3: fp32 out += acc (atomic; k_splits > 1 allowed).
+ * Row pitches (elements) multiples of 8 and A, B 16-byte aligned; device error bits are OR-ed into
+ * *d_status. */
+int sf_gemm_bf16(int32_t M, int32_t N, int32_t K, const uint16_t *A, int32_t lda, int32_t a_mn_major,
+                 const uint16_t *B, int32_t ldb, int32_t b_mn_major, int32_t epilogue, const float *bias,
+                 const uint16_t *mask, int32_t ldm, void *out, int32_t ldo, int32_t k_splits, uint32_t *d_status,
+                 void *stream);
+/* The learned eigen stage in place of sf_covariance_eig (SF_EIG_SAME_POL_WHITENED): features ->
+ * MLP -> n_iter subspace iterations U <- orth(A U) from its four start vectors -> Rayleigh-Ritz
+ * (4 x 4 complex Jacobi) -> K (fixed, or theta > delta x noise floor with the floor
+ * (tr A - sum theta) / (n - 4)) -> the plan's effective weights with I - U_K U_K^H.  A matrix
+ * whose residual ||A u_k - theta_k u_k|| exceeds tol x theta_0, whose K exceeds 4, or whose rule
+ * needs every eigenvalue (SF_K_DETECT) is listed on the device and solved by the full top-K
+ * eigensolver instead, so it gets exactly the plain chain's weights.  d_ritz float [2C][4] and
+ * d_fallback_count (one int32, the number of rejected matrices) may be NULL. */
+int sf_covariance_eig_learned(sf_plan *plan, sf_proposer *proposer, const int32_t *d_vis, int32_t k_rule,
+                              float delta, int32_t n_iter, float tol, int32_t *d_counts, float *d_ritz,
+                              int32_t *d_fallback_count, void *stream);
+/* correlate -> learned eigen stage -> beams (2B per pol), as sf_run_adaptive. */
+int sf_run_adaptive_learned(sf_plan *plan, sf_proposer *proposer, const int8_t *d_samples,
+                            const int16_t *d_scales, int32_t k_rule, float delta, int32_t n_iter, float tol,
+                            int32_t *d_vis, int32_t *d_counts, uint16_t *d_beams_f16,
+                            int32_t *d_fallback_count, void *stream);
+
 /* ---- allocation-free variant ------------------------------------------------ */
 
 /* The adaptive chain of sf_run_adaptive for callers that cannot allocate
