@@ -31,6 +31,7 @@
 // tridiagonalisation of a Hermitian matrix), Sturm sequences (eigenvalue
 // counts of a symmetric tridiagonal) with bisection / multisection, inverse
 // iteration with partial pivoting and modified Gram-Schmidt.
+#include <algorithm>
 #include <cstdio>
 
 #include "sf_common.cuh"
@@ -236,12 +237,10 @@ __device__ __forceinline__ float2 rank2(float2 r, const float4 &qi, const float4
   return r;
 }
 
-__global__ void __launch_bounds__(NT, 6) sf_eig_small_kernel(const SmallEigArgs a) {
-  extern __shared__ __align__(16) uint8_t smem[];
+// the whole solve of matrix bt (c * 2 + p) by the CTA
+__device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, int bt, uint8_t *smem) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int rs = tid >> 2, sg = tid & 3;  // row slot, column segment
-  if (a.list ? (int)blockIdx.x >= *a.list_count : (int)blockIdx.x >= 2 * a.C) return;
-  const int bt = a.list ? a.list[blockIdx.x] : (int)blockIdx.x;  // c * 2 + p
   const int n = a.R, B = a.B, ld = small_ld(n);
   const int c = bt >> 1, p = bt & 1;
   const SRegion L = s_region(n, B);
@@ -774,6 +773,17 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_small_kernel(const SmallEigArgs 
   }
 }
 
+// One CTA per matrix, or in list mode a grid of at most one resident wave
+// walking list[0 .. *list_count) (the count is known only on the device)
+__global__ void __launch_bounds__(NT, 6) sf_eig_small_kernel(const SmallEigArgs a) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int count = a.list ? *a.list_count : 2 * a.C;
+  for (int slot = blockIdx.x; slot < count; slot += gridDim.x) {
+    eig_small_one(a, a.list ? a.list[slot] : slot, smem);
+    __syncthreads();  // the next matrix reuses the shared memory
+  }
+}
+
 }  // namespace
 
 int sf_eig_small_supported(const sf_plan *p) {
@@ -804,7 +814,13 @@ cudaError_t sf_launch_eig_small(const sf_plan *p, const int32_t *vis, int k_rule
   const size_t smem = s_region(p->R, p->B).total;
   cudaError_t e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_small_kernel), smem);
   if (e != cudaSuccess) return e;
-  // one CTA per matrix (list mode: as many CTAs as the list can hold, the rest return at once)
-  sf_eig_small_kernel<<<2 * p->C, NT, smem, stream>>>(a);
+  int grid = 2 * p->C;
+  if (list) {
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sf_eig_small_kernel, NT, smem);
+    if (e != cudaSuccess) return e;
+    grid = std::min(grid, std::max(1, per_sm) * p->num_sms);
+  }
+  sf_eig_small_kernel<<<grid, NT, smem, stream>>>(a);
   return cudaGetLastError();
 }

@@ -45,6 +45,7 @@ namespace {
 constexpr int KV = 4;        // proposed vectors per matrix
 constexpr int RR_MAX_N = 64;
 constexpr int RR_NPL = 2;    // rows per lane (n <= 64)
+constexpr int W_B_MAX_RR = 16;  // beams per pol
 
 int fail(int code, const char *fmt, ...) {
   char buf[320];
@@ -94,6 +95,12 @@ __global__ void sf_proposer_features_kernel(const int32_t *vis, int R, int NBL, 
   for (int k = 2 * NBL + threadIdx.x; k < ldx; k += blockDim.x) xr[k] = __float2bfloat16_rn(0.0f);
 }
 
+// bytes of one warp's region: A n x (n + 1), U and V 4 n, W0 B n, factors n (float2), s n (float)
+__host__ __device__ inline size_t rr_region(int n, int B) {
+  const size_t per = ((size_t)n * (n + 1) + 2 * (size_t)KV * n + (size_t)B * n + (size_t)n) * 8 + (size_t)n * 4;
+  return (per + 15) & ~size_t(15);
+}
+
 struct RRArgs {
   const int32_t *vis;
   const float2 *factors;
@@ -112,7 +119,9 @@ struct RRArgs {
   float tol;
 };
 
-// One warp per (channel, pol) matrix; `wpc` matrices per CTA.
+// One warp per (channel, pol) matrix; `wpc` matrices per CTA.  Every group of
+// independent sums shares one shuffle butterfly (the kernel is bound by the
+// latency of its dependent steps, not by arithmetic).
 __global__ void __launch_bounds__(128) sf_rr_kernel(const RRArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -120,85 +129,146 @@ __global__ void __launch_bounds__(128) sf_rr_kernel(const RRArgs a) {
   if (row >= a.rows) return;
   const int n = a.R, ld = n + 1, B = a.B;
   const int c = row >> 1, p = row & 1;
-  // per-warp region: A n x ld, U 4 n, V 4 n, s n (float), W0 B n
-  const size_t per = (size_t)n * ld * 8 + 2 * (size_t)KV * n * 8 + (size_t)n * 4 + (size_t)B * n * 8 + 16;
-  uint8_t *base = smem + warp * ((per + 15) & ~size_t(15));
+  uint8_t *base = smem + warp * rr_region(n, B);
   float2 *A = reinterpret_cast<float2 *>(base);
   float2 *U = A + n * ld;
   float2 *V = U + KV * n;
   float2 *W0 = V + KV * n;
-  float *s = reinterpret_cast<float *>(W0 + B * n);
-  const int32_t *vb = a.vis + (size_t)c * a.NBL * 8;
+  float2 *fac = W0 + B * n;
+  float *s = reinterpret_cast<float *>(fac + n);
+  // same-pol entry (p, p) of baseline b at vin[8 b], vin[8 b + 1] (layout [b][Pol][Pol][2])
+  const int32_t *vin = a.vis + (size_t)c * a.NBL * 8 + 6 * p;
   const float2 *dp = a.factors + (size_t)row * n;
+  const bool r0 = lane < n, r1 = lane + 32 < n;  // this lane's rows lane, lane + 32
 
   // whitened covariance with the receiver factors, both triangles
   for (int i = lane; i < n; i += 32) {
-    const int32_t *v = vb + ((size_t)baseline_of(i, i) * 2 + p) * 4 + p * 2;
     const float2 d = dp[i];
-    s[i] = sqrtf(fmaxf(static_cast<float>(v[0]) * (d.x * d.x + d.y * d.y), 1e-10f));
+    fac[i] = d;
+    s[i] = sqrtf(fmaxf(static_cast<float>(vin[(size_t)baseline_of(i, i) * 8]) * (d.x * d.x + d.y * d.y), 1e-10f));
   }
   __syncwarp();
-  for (int e = lane; e < n * n; e += 32) {
-    const int i = e / n, j = e - (e / n) * n;
-    if (j < i) continue;
-    const int32_t *v = vb + ((size_t)baseline_of(i, j) * 2 + p) * 4 + p * 2;
-    float2 x = make_float2(static_cast<float>(v[0]), static_cast<float>(v[1]));
-    x = cmulc(cmul(dp[i], x), dp[j]);  // d_i V(i, j) conj(d_j), element (i, j)
-    const float inv = 1.0f / (s[i] * s[j]);
-    A[i * ld + j] = i == j ? make_float2(x.x * inv, 0.0f) : make_float2(x.x * inv, x.y * inv);
-    if (j > i) A[j * ld + i] = make_float2(x.x * inv, -x.y * inv);
+  {
+    const int nb = n * (n + 1) / 2;
+    for (int b0 = 0; b0 < nb; b0 += 8 * 32) {
+      int2 raw[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int b = b0 + u * 32 + lane;
+        raw[u] = b < nb ? *reinterpret_cast<const int2 *>(vin + (size_t)b * 8) : make_int2(0, 0);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int b = b0 + u * 32 + lane;
+        if (b < nb) {
+          int j = static_cast<int>((sqrtf(8.0f * static_cast<float>(b) + 1.0f) - 1.0f) * 0.5f);
+          if ((j + 1) * (j + 2) / 2 <= b) ++j;
+          if (j * (j + 1) / 2 > b) --j;
+          const int i = b - j * (j + 1) / 2;
+          float2 x = make_float2(static_cast<float>(raw[u].x), static_cast<float>(raw[u].y));
+          x = cmulc(cmul(fac[i], x), fac[j]);  // d_i V(i, j) conj(d_j), element (i, j)
+          const float inv = 1.0f / (s[i] * s[j]);
+          A[i * ld + j] = i == j ? make_float2(x.x * inv, 0.0f) : make_float2(x.x * inv, x.y * inv);
+          if (j > i) A[j * ld + i] = make_float2(x.x * inv, -x.y * inv);
+        }
+      }
+    }
   }
   // start vectors: the MLP's (for the factor-free covariance) turned by the factors' phases
-  const float *yr = a.y + (size_t)row * a.ldy;
-  for (int e = lane; e < KV * n; e += 32) {
-    const int k = e / n, i = e - k * n;
-    const float2 d = dp[i];
-    const float dm = sqrtf(d.x * d.x + d.y * d.y);
-    const float2 ph = dm > 0.0f ? make_float2(d.x / dm, d.y / dm) : make_float2(1.0f, 0.0f);
-    U[e] = cmul(make_float2(yr[k * 2 * n + 2 * i], yr[k * 2 * n + 2 * i + 1]), ph);
+  {
+    const float2 *yr = reinterpret_cast<const float2 *>(a.y + (size_t)row * a.ldy);  // ldy even
+    float2 yv[KV][RR_NPL];
+#pragma unroll
+    for (int k = 0; k < KV; ++k)
+#pragma unroll
+      for (int t = 0; t < RR_NPL; ++t) {
+        const int i = lane + 32 * t;
+        yv[k][t] = i < n ? yr[k * n + i] : make_float2(0.0f, 0.0f);
+      }
+    const __half2 *w = a.weights + (size_t)row * B * n;
+    __half2 wv[(W_B_MAX_RR * RR_MAX_N) / 32];
+#pragma unroll
+    for (int q = 0; q < (W_B_MAX_RR * RR_MAX_N) / 32; ++q) {
+      const int e = lane + 32 * q;
+      if (e < B * n) wv[q] = w[e];
+    }
+#pragma unroll
+    for (int t = 0; t < RR_NPL; ++t) {
+      const int i = lane + 32 * t;
+      if (i < n) {
+        const float2 d = fac[i];
+        const float dm2 = d.x * d.x + d.y * d.y;
+        const float rm = dm2 > 0.0f ? rsqrtf(dm2) : 0.0f;
+        const float2 ph = dm2 > 0.0f ? make_float2(d.x * rm, d.y * rm) : make_float2(1.0f, 0.0f);
+#pragma unroll
+        for (int k = 0; k < KV; ++k) U[k * n + i] = cmul(yv[k][t], ph);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < (W_B_MAX_RR * RR_MAX_N) / 32; ++q) {
+      const int e = lane + 32 * q;
+      if (e < B * n) W0[e] = __half22float2(wv[q]);
+    }
   }
-  const __half2 *w = a.weights + (size_t)row * B * n;
-  for (int e = lane; e < B * n; e += 32) W0[e] = __half22float2(w[e]);
   __syncwarp();
 
-  // modified Gram-Schmidt of the four vectors in X (n x 4), two projection
-  // rounds; a vector that vanishes is replaced by a fixed unit vector and
-  // orthogonalised again
+  // orthonormal basis of the four vectors in X (n x 4): classical Gram-Schmidt
+  // twice, the dots of vector k with the earlier ones reduced together; a
+  // vector that vanishes is replaced by a fixed unit vector and redone
   auto orth = [&](float2 *X) {
+#pragma unroll
     for (int k = 0; k < KV; ++k) {
+      float2 xl0[KV], xl1[KV];
+#pragma unroll
+      for (int l = 0; l < KV; ++l) {
+        xl0[l] = l < k && r0 ? X[l * n + lane] : make_float2(0.0f, 0.0f);
+        xl1[l] = l < k && r1 ? X[l * n + lane + 32] : make_float2(0.0f, 0.0f);
+      }
       for (int attempt = 0; attempt < 2; ++attempt) {
-        for (int round = 0; round < 2; ++round)
-          for (int l = 0; l < k; ++l) {
-            float cr = 0.0f, ci = 0.0f;  // <x_l, x_k>
-            for (int i = lane; i < n; i += 32) {
-              const float2 xl = X[l * n + i], xk = X[k * n + i];
-              cr += xl.x * xk.x + xl.y * xk.y;
-              ci += xl.x * xk.y - xl.y * xk.x;
+        float2 x0 = r0 ? X[k * n + lane] : make_float2(0.0f, 0.0f);
+        float2 x1 = r1 ? X[k * n + lane + 32] : make_float2(0.0f, 0.0f);
+        if (attempt > 0) {
+          const int e1 = (k * 7 + 2 + attempt) % n;
+          x0 = make_float2(lane == e1 ? 1.0f : 0.0f, 0.0f);
+          x1 = make_float2(lane + 32 == e1 ? 1.0f : 0.0f, 0.0f);
+        }
+        if (k > 0) {
+#pragma unroll
+          for (int round = 0; round < 2; ++round) {
+            float dr[KV - 1], di[KV - 1];  // <x_l, x_k>
+#pragma unroll
+            for (int l = 0; l < KV - 1; ++l) {
+              dr[l] = xl0[l].x * x0.x + xl0[l].y * x0.y + xl1[l].x * x1.x + xl1[l].y * x1.y;
+              di[l] = xl0[l].x * x0.y - xl0[l].y * x0.x + xl1[l].x * x1.y - xl1[l].y * x1.x;
             }
-            cr = wsum(cr);
-            ci = wsum(ci);
-            for (int i = lane; i < n; i += 32) {
-              const float2 xl = X[l * n + i];
-              X[k * n + i].x -= cr * xl.x - ci * xl.y;
-              X[k * n + i].y -= cr * xl.y + ci * xl.x;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+              for (int l = 0; l < KV - 1; ++l) {
+                dr[l] += __shfl_xor_sync(0xffffffffu, dr[l], o);
+                di[l] += __shfl_xor_sync(0xffffffffu, di[l], o);
+              }
             }
-            __syncwarp();
+#pragma unroll
+            for (int l = 0; l < KV - 1; ++l) {
+              if (l < k) {
+                x0.x -= dr[l] * xl0[l].x - di[l] * xl0[l].y;
+                x0.y -= dr[l] * xl0[l].y + di[l] * xl0[l].x;
+                x1.x -= dr[l] * xl1[l].x - di[l] * xl1[l].y;
+                x1.y -= dr[l] * xl1[l].y + di[l] * xl1[l].x;
+              }
+            }
           }
-        float nr = 0.0f;
-        for (int i = lane; i < n; i += 32) nr += X[k * n + i].x * X[k * n + i].x + X[k * n + i].y * X[k * n + i].y;
-        nr = wsum(nr);
-        if (nr > 1e-20f) {
-          const float inv = rsqrtf(nr);
-          for (int i = lane; i < n; i += 32) {
-            X[k * n + i].x *= inv;
-            X[k * n + i].y *= inv;
-          }
-          __syncwarp();
+        }
+        const float nr = wsum(x0.x * x0.x + x0.y * x0.y + x1.x * x1.x + x1.y * x1.y);
+        if (nr > 1e-20f || attempt == 1) {
+          const float inv = nr > 1e-20f ? rsqrtf(nr) : 0.0f;
+          if (r0) X[k * n + lane] = make_float2(x0.x * inv, x0.y * inv);
+          if (r1) X[k * n + lane + 32] = make_float2(x1.x * inv, x1.y * inv);
           break;
         }
-        for (int i = lane; i < n; i += 32) X[k * n + i] = make_float2(i == (k * 7 + 3 + attempt) % n ? 1.0f : 0.0f, 0.0f);
-        __syncwarp();
       }
+      __syncwarp();
     }
   };
   // V = A U (lane: rows lane, lane + 32)
@@ -208,21 +278,40 @@ __global__ void __launch_bounds__(128) sf_rr_kernel(const RRArgs a) {
     for (int t = 0; t < RR_NPL; ++t)
 #pragma unroll
       for (int k = 0; k < KV; ++k) acc[t][k] = make_float2(0.0f, 0.0f);
-    for (int j = 0; j < n; ++j) {
-      float2 uj[KV];
+    int j = 0;
+    for (; j + 1 < n; j += 2) {
+      float2 uj[2][KV], aij[2][RR_NPL];
 #pragma unroll
-      for (int k = 0; k < KV; ++k) uj[k] = U[k * n + j];
+      for (int h = 0; h < 2; ++h) {
 #pragma unroll
-      for (int t = 0; t < RR_NPL; ++t) {
-        const int i = lane + 32 * t;
-        if (i < n) {
-          const float2 aij = A[i * ld + j];
+        for (int k = 0; k < KV; ++k) uj[h][k] = U[k * n + j + h];
+#pragma unroll
+        for (int t = 0; t < RR_NPL; ++t) {
+          const int i = lane + 32 * t;
+          aij[h][t] = i < n ? A[i * ld + j + h] : make_float2(0.0f, 0.0f);
+        }
+      }
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int t = 0; t < RR_NPL; ++t)
 #pragma unroll
           for (int k = 0; k < KV; ++k) {
-            const float2 pr = cmul(aij, uj[k]);
+            const float2 pr = cmul(aij[h][t], uj[h][k]);
             acc[t][k].x += pr.x;
             acc[t][k].y += pr.y;
           }
+    }
+    if (j < n) {
+#pragma unroll
+      for (int t = 0; t < RR_NPL; ++t) {
+        const int i = lane + 32 * t;
+        const float2 aj = i < n ? A[i * ld + j] : make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int k = 0; k < KV; ++k) {
+          const float2 pr = cmul(aj, U[k * n + j]);
+          acc[t][k].x += pr.x;
+          acc[t][k].y += pr.y;
         }
       }
     }
@@ -244,20 +333,51 @@ __global__ void __launch_bounds__(128) sf_rr_kernel(const RRArgs a) {
     orth(U);
   }
   apply();
-  // H = U^H A U (Hermitian 4 x 4), every lane a copy
+  // H = U^H A U (Hermitian 4 x 4), every lane a copy: the 10 entries k <= l in one reduction
   float2 H[KV][KV];
+  {
+    float hv[2 * KV * KV];
 #pragma unroll
-  for (int k = 0; k < KV; ++k)
+    for (int q = 0; q < 2 * KV * KV; ++q) hv[q] = 0.0f;
 #pragma unroll
-    for (int l = 0; l < KV; ++l) {
-      float hr = 0.0f, hi = 0.0f;  // conj(u_k) . v_l
-      for (int i = lane; i < n; i += 32) {
-        const float2 uk = U[k * n + i], vl = V[l * n + i];
-        hr += uk.x * vl.x + uk.y * vl.y;
-        hi += uk.x * vl.y - uk.y * vl.x;
+    for (int t = 0; t < RR_NPL; ++t) {
+      const int i = lane + 32 * t;
+      if (i < n) {
+        float2 uk[KV], vl[KV];
+#pragma unroll
+        for (int k = 0; k < KV; ++k) {
+          uk[k] = U[k * n + i];
+          vl[k] = V[k * n + i];
+        }
+#pragma unroll
+        for (int k = 0; k < KV; ++k)
+#pragma unroll
+          for (int l = k; l < KV; ++l) {  // conj(u_k) . v_l
+            hv[2 * (k * KV + l)] += uk[k].x * vl[l].x + uk[k].y * vl[l].y;
+            hv[2 * (k * KV + l) + 1] += uk[k].x * vl[l].y - uk[k].y * vl[l].x;
+          }
       }
-      H[k][l] = make_float2(wsum(hr), wsum(hi));
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int k = 0; k < KV; ++k)
+#pragma unroll
+        for (int l = k; l < KV; ++l) {
+          hv[2 * (k * KV + l)] += __shfl_xor_sync(0xffffffffu, hv[2 * (k * KV + l)], o);
+          hv[2 * (k * KV + l) + 1] += __shfl_xor_sync(0xffffffffu, hv[2 * (k * KV + l) + 1], o);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < KV; ++k)
+#pragma unroll
+      for (int l = k; l < KV; ++l) {
+        H[k][l] = make_float2(hv[2 * (k * KV + l)], hv[2 * (k * KV + l) + 1]);
+        H[l][k] = make_float2(H[k][l].x, -H[k][l].y);
+      }
+#pragma unroll
+    for (int k = 0; k < KV; ++k) H[k][k].y = 0.0f;
+  }
   // cyclic Jacobi on the 4 x 4 Hermitian H: J = I except J_pp = c, J_pq = s,
   // J_qp = -s conj(e), J_qq = c conj(e) with H_pq = g e (|e| = 1),
   // t = sign(tau) / (|tau| + sqrt(1 + tau^2)), tau = (H_qq - H_pp) / (2 g)
@@ -281,11 +401,13 @@ __global__ void __launch_bounds__(128) sf_rr_kernel(const RRArgs a) {
 #pragma unroll
       for (int qq = pp + 1; qq < KV; ++qq) {
         const float2 h = H[pp][qq];
-        const float g = sqrtf(h.x * h.x + h.y * h.y);
-        if (g < 1e-30f) continue;
-        const float2 e = make_float2(h.x / g, h.y / g);
-        const float tau = (H[qq][qq].x - H[pp][pp].x) / (2.0f * g);
-        const float t = (tau >= 0.0f ? 1.0f : -1.0f) / (fabsf(tau) + sqrtf(1.0f + tau * tau));
+        const float g2 = h.x * h.x + h.y * h.y;
+        if (!(g2 > 1e-36f)) continue;  // |H_pq| below 1e-18: nothing to rotate
+        const float rg = rsqrtf(g2);
+        const float2 e = make_float2(h.x * rg, h.y * rg);
+        const float tau = (H[qq][qq].x - H[pp][pp].x) * (0.5f * rg);
+        const float tau2 = 1.0f + tau * tau;
+        const float t = __fdividef(tau >= 0.0f ? 1.0f : -1.0f, fabsf(tau) + tau2 * rsqrtf(tau2));
         const float cs = rsqrtf(1.0f + t * t), sn = t * cs;
         const float2 ce = make_float2(e.x, -e.y);  // conj(e)
         // columns: col p' = c col p - s conj(e) col q ; col q' = s col p + c conj(e) col q
@@ -310,27 +432,35 @@ __global__ void __launch_bounds__(128) sf_rr_kernel(const RRArgs a) {
         }
       }
   }
-  // Ritz values descending, Ritz vectors U Q, A U Q
-  int ord[KV];
-  float th[KV];
+  // Ritz values descending, Ritz vectors U Q, A U Q (kept in registers for the residuals)
+  // (a compare-exchange network on values, so nothing is indexed at run time)
+  float theta[KV];
 #pragma unroll
-  for (int k = 0; k < KV; ++k) {
-    ord[k] = k;
-    th[k] = H[k][k].x;
-  }
+  for (int k = 0; k < KV; ++k) theta[k] = H[k][k].x;
 #pragma unroll
-  for (int k = 0; k < KV; ++k)
+  for (int pass = 0; pass < KV - 1; ++pass)
 #pragma unroll
     for (int l = 0; l < KV - 1; ++l)
-      if (th[ord[l]] < th[ord[l + 1]]) {
-        const int tmp = ord[l];
-        ord[l] = ord[l + 1];
-        ord[l + 1] = tmp;
+      if (theta[l] < theta[l + 1]) {
+        const float tt = theta[l];
+        theta[l] = theta[l + 1];
+        theta[l + 1] = tt;
+#pragma unroll
+        for (int r = 0; r < KV; ++r) {  // the Ritz vectors' coefficients follow their values
+          const float2 tq = Q[r][l];
+          Q[r][l] = Q[r][l + 1];
+          Q[r][l + 1] = tq;
+        }
       }
+  // trace and the residuals ||A u_k - theta_k u_k||^2 in one reduction
+  float rs[KV + 1];
+#pragma unroll
+  for (int k = 0; k <= KV; ++k) rs[k] = 0.0f;
 #pragma unroll
   for (int t = 0; t < RR_NPL; ++t) {
     const int i = lane + 32 * t;
     if (i >= n) continue;
+    rs[KV] += A[i * ld + i].x;
     float2 uo[KV], vo[KV];
 #pragma unroll
     for (int k = 0; k < KV; ++k) {
@@ -342,7 +472,7 @@ __global__ void __launch_bounds__(128) sf_rr_kernel(const RRArgs a) {
       float2 un = make_float2(0.0f, 0.0f), vn = make_float2(0.0f, 0.0f);
 #pragma unroll
       for (int l = 0; l < KV; ++l) {
-        const float2 q = Q[l][ord[k]];
+        const float2 q = Q[l][k];
         const float2 a1 = cmul(uo[l], q), a2 = cmul(vo[l], q);
         un.x += a1.x;
         un.y += a1.y;
@@ -350,25 +480,20 @@ __global__ void __launch_bounds__(128) sf_rr_kernel(const RRArgs a) {
         vn.y += a2.y;
       }
       U[k * n + i] = un;
-      V[k * n + i] = vn;
+      const float dx = vn.x - theta[k] * un.x, dy = vn.y - theta[k] * un.y;
+      rs[k] += dx * dx + dy * dy;
     }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int k = 0; k <= KV; ++k) rs[k] += __shfl_xor_sync(0xffffffffu, rs[k], o);
   }
   __syncwarp();
-  float theta[KV], res[KV];
-  float trace = 0.0f;
-  for (int i = lane; i < n; i += 32) trace += A[i * ld + i].x;
-  trace = wsum(trace);
+  const float trace = rs[KV];
+  float res[KV];
 #pragma unroll
-  for (int k = 0; k < KV; ++k) {
-    theta[k] = th[ord[k]];
-    float r2 = 0.0f;
-    for (int i = lane; i < n; i += 32) {
-      const float2 v = V[k * n + i], u = U[k * n + i];
-      const float dx = v.x - theta[k] * u.x, dy = v.y - theta[k] * u.y;
-      r2 += dx * dx + dy * dy;
-    }
-    res[k] = sqrtf(wsum(r2));
-  }
+  for (int k = 0; k < KV; ++k) res[k] = sqrtf(rs[k]);
   const float floor_est = (trace - (theta[0] + theta[1] + theta[2] + theta[3])) / static_cast<float>(n - KV);
   int K = 0;
   bool accept = true;
@@ -384,9 +509,16 @@ __global__ void __launch_bounds__(128) sf_rr_kernel(const RRArgs a) {
     accept = false;  // the percentile rule needs every eigenvalue
   }
   const float anorm = fmaxf(theta[0], 1e-30f);
-  for (int k = 0; k < KV && accept; ++k)
+#pragma unroll
+  for (int k = 0; k < KV; ++k)
     if (k < K && !(res[k] <= a.tol * anorm)) accept = false;
-  if (a.ritz && lane < KV) a.ritz[(size_t)row * KV + lane] = theta[lane];
+  if (a.ritz && lane < KV) {
+    float tl = theta[0];
+#pragma unroll
+    for (int k = 1; k < KV; ++k)
+      if (lane == k) tl = theta[k];
+    a.ritz[(size_t)row * KV + lane] = tl;
+  }
   if (!accept) {
     if (lane == 0) {
       const int slot = atomicAdd(a.fb_count, 1);
@@ -395,47 +527,83 @@ __global__ void __launch_bounds__(128) sf_rr_kernel(const RRArgs a) {
     return;
   }
   if (lane == 0 && a.counts) a.counts[row] = K;
-  // un-whiten and normalise the kept vectors, then W' = W - sum_k (W z_k) z_k^H
-  for (int k = 0; k < K; ++k) {
-    float nr = 0.0f;
-    for (int i = lane; i < n; i += 32) {
-      float2 z = U[k * n + i];
-      z.x *= s[i];
-      z.y *= s[i];
-      U[k * n + i] = z;
-      nr += z.x * z.x + z.y * z.y;
-    }
-    nr = wsum(nr);
-    const float inv = nr > 0.0f ? rsqrtf(nr) : 0.0f;
-    for (int i = lane; i < n; i += 32) {
-      U[k * n + i].x *= inv;
-      U[k * n + i].y *= inv;
-    }
-  }
-  __syncwarp();
-  float2 *we = a.weff + (size_t)row * 2 * B * n;
-  for (int m = 0; m < B; ++m) {
-    float2 cf[KV];
+  // un-whiten and normalise the kept vectors (norms in one reduction), then
+  // W' = W - sum_k (W z_k) z_k^H with the coefficients of four beams per reduction
+  float2 z0[KV], z1[KV];
+  {
+    const float s0 = r0 ? s[lane] : 0.0f, s1 = r1 ? s[lane + 32] : 0.0f;
+    float nr[KV];
 #pragma unroll
     for (int k = 0; k < KV; ++k) {
-      float cr = 0.0f, ci = 0.0f;
-      if (k < K)
-        for (int i = lane; i < n; i += 32) {
-          const float2 pr = cmul(W0[m * n + i], U[k * n + i]);
-          cr += pr.x;
-          ci += pr.y;
-        }
-      cf[k] = make_float2(wsum(cr), wsum(ci));
+      z0[k] = k < K && r0 ? U[k * n + lane] : make_float2(0.0f, 0.0f);
+      z1[k] = k < K && r1 ? U[k * n + lane + 32] : make_float2(0.0f, 0.0f);
+      z0[k] = make_float2(z0[k].x * s0, z0[k].y * s0);
+      z1[k] = make_float2(z1[k].x * s1, z1[k].y * s1);
+      nr[k] = z0[k].x * z0[k].x + z0[k].y * z0[k].y + z1[k].x * z1[k].x + z1[k].y * z1[k].y;
     }
-    for (int i = lane; i < n; i += 32) {
-      float2 wp = W0[m * n + i];
-      for (int k = 0; k < K; ++k) {
-        const float2 t = cmulc(cf[k], U[k * n + i]);  // c conj(z_i)
-        wp.x -= t.x;
-        wp.y -= t.y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int k = 0; k < KV; ++k) nr[k] += __shfl_xor_sync(0xffffffffu, nr[k], o);
+    }
+#pragma unroll
+    for (int k = 0; k < KV; ++k) {
+      const float inv = nr[k] > 0.0f ? rsqrtf(nr[k]) : 0.0f;
+      z0[k] = make_float2(z0[k].x * inv, z0[k].y * inv);
+      z1[k] = make_float2(z1[k].x * inv, z1[k].y * inv);
+    }
+  }
+  float2 *we = a.weff + (size_t)row * 2 * B * n;
+  const float2 f0 = r0 ? fac[lane] : make_float2(0.0f, 0.0f), f1 = r1 ? fac[lane + 32] : make_float2(0.0f, 0.0f);
+  for (int m0 = 0; m0 < B; m0 += 4) {
+    float cr[4][KV], ci[4][KV];
+    float2 wa[4], wb[4];
+#pragma unroll
+    for (int mm = 0; mm < 4; ++mm) {
+      const bool on = m0 + mm < B;
+      wa[mm] = on && r0 ? W0[(m0 + mm) * n + lane] : make_float2(0.0f, 0.0f);
+      wb[mm] = on && r1 ? W0[(m0 + mm) * n + lane + 32] : make_float2(0.0f, 0.0f);
+#pragma unroll
+      for (int k = 0; k < KV; ++k) {  // W_m . z_k
+        const float2 p0 = cmul(wa[mm], z0[k]), p1 = cmul(wb[mm], z1[k]);
+        cr[mm][k] = p0.x + p1.x;
+        ci[mm][k] = p0.y + p1.y;
       }
-      we[m * n + i] = cmul(W0[m * n + i], dp[i]);
-      we[B * n + m * n + i] = cmul(wp, dp[i]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int mm = 0; mm < 4; ++mm)
+#pragma unroll
+        for (int k = 0; k < KV; ++k) {
+          cr[mm][k] += __shfl_xor_sync(0xffffffffu, cr[mm][k], o);
+          ci[mm][k] += __shfl_xor_sync(0xffffffffu, ci[mm][k], o);
+        }
+    }
+#pragma unroll
+    for (int mm = 0; mm < 4; ++mm) {
+      const int m = m0 + mm;
+      if (m >= B) continue;
+      float2 pa = wa[mm], pb = wb[mm];
+#pragma unroll
+      for (int k = 0; k < KV; ++k) {
+        if (k < K) {
+          const float2 cf = make_float2(cr[mm][k], ci[mm][k]);
+          const float2 t0 = cmulc(cf, z0[k]), t1 = cmulc(cf, z1[k]);  // c conj(z_i)
+          pa.x -= t0.x;
+          pa.y -= t0.y;
+          pb.x -= t1.x;
+          pb.y -= t1.y;
+        }
+      }
+      if (r0) {
+        we[m * n + lane] = cmul(wa[mm], f0);
+        we[B * n + m * n + lane] = cmul(pa, f0);
+      }
+      if (r1) {
+        we[m * n + lane + 32] = cmul(wb[mm], f1);
+        we[B * n + m * n + lane + 32] = cmul(pb, f1);
+      }
     }
   }
 }
@@ -485,10 +653,7 @@ void free_proposer(sf_proposer *q) {
   delete q;
 }
 
-size_t rr_smem_per_warp(int n, int B) {
-  const size_t per = (size_t)n * (n + 1) * 8 + 2 * (size_t)KV * n * 8 + (size_t)n * 4 + (size_t)B * n * 8 + 16;
-  return (per + 15) & ~size_t(15);
-}
+size_t rr_smem_per_warp(int n, int B) { return rr_region(n, B); }
 
 }  // namespace
 
