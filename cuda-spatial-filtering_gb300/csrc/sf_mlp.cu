@@ -161,39 +161,85 @@ __global__ void __launch_bounds__(GTHREADS, 1)
     tc_fence_after();
     const int m = m0 + q * 32 + lane;
     const uint32_t taddr = h.tmem_base + (static_cast<uint32_t>(q * 32) << 16);
+    // a row's 16 columns go out as 16-byte stores when the pitch and the chunk allow it
+    const bool vec_bf16 = (a.ldo % 8) == 0 && (reinterpret_cast<uintptr_t>(a.out) % 16) == 0;
+    const bool vec_f32 = (a.ldo % 4) == 0 && (reinterpret_cast<uintptr_t>(a.out) % 16) == 0;
+    const bool vec_mask = a.mask && (a.ldm % 8) == 0 && (reinterpret_cast<uintptr_t>(a.mask) % 16) == 0;
+    uint32_t nxt[16];
+    tmem_ld16(taddr, nxt);
     for (int cb = 0; cb < GT / 16; ++cb) {
       uint32_t v[16];
-      tmem_ld16(taddr + cb * 16, v);
+      __syncwarp();  // converged for the warp-wide tensor-memory operations
       tmem_wait_ld();
+#pragma unroll
+      for (int e = 0; e < 16; ++e) v[e] = nxt[e];
+      if (cb + 1 < GT / 16) tmem_ld16(taddr + (cb + 1) * 16, nxt);  // next chunk in flight
       if (!ok || nkb == 0 || m >= a.M) continue;
       const int nb = n0 + cb * 16;
       if (nb >= a.N) continue;
+      const bool full = nb + 16 <= a.N;
+      float x[16];
+#pragma unroll
+      for (int e = 0; e < 16; ++e) x[e] = __uint_as_float(v[e]);
       if (a.mode == 3) {
         float *o = static_cast<float *>(a.out) + (size_t)m * a.ldo + nb;
 #pragma unroll
         for (int e = 0; e < 16; ++e)
-          if (nb + e < a.N) atomicAdd(o + e, __uint_as_float(v[e]));
-      } else if (a.mode == 1) {
+          if (nb + e < a.N) atomicAdd(o + e, x[e]);
+        continue;
+      }
+      if ((a.mode == 0 || a.mode == 1) && a.bias) {
+#pragma unroll
+        for (int e = 0; e < 16; ++e) x[e] += nb + e < a.N ? a.bias[nb + e] : 0.0f;
+      }
+      if (a.mode == 1) {
         float *o = static_cast<float *>(a.out) + (size_t)m * a.ldo + nb;
+        if (full && vec_f32) {
 #pragma unroll
-        for (int e = 0; e < 16; ++e)
-          if (nb + e < a.N) o[e] = __uint_as_float(v[e]) + (a.bias ? a.bias[nb + e] : 0.0f);
-      } else {
-        __nv_bfloat16 *o = static_cast<__nv_bfloat16 *>(a.out) + (size_t)m * a.ldo + nb;
+          for (int e = 0; e < 16; e += 4) *reinterpret_cast<float4 *>(o + e) = make_float4(x[e], x[e + 1], x[e + 2], x[e + 3]);
+        } else {
 #pragma unroll
-        for (int e = 0; e < 16; ++e) {
-          if (nb + e >= a.N) continue;
-          float x = __uint_as_float(v[e]);
-          if (a.mode == 0) {
-            x = fmaxf(x + (a.bias ? a.bias[nb + e] : 0.0f), 0.0f);
-          } else if (a.mode == 2) {
-            const float mk = __bfloat162float(a.mask[(size_t)m * a.ldm + nb + e]);
-            x = mk > 0.0f ? x : 0.0f;
-          }
-          o[e] = __float2bfloat16_rn(x);
+          for (int e = 0; e < 16; ++e)
+            if (nb + e < a.N) o[e] = x[e];
+        }
+        continue;
+      }
+      if (a.mode == 0) {
+#pragma unroll
+        for (int e = 0; e < 16; ++e) x[e] = fmaxf(x[e], 0.0f);
+      } else {  // mode 2: back through a ReLU
+        const __nv_bfloat16 *mk = a.mask + (size_t)m * a.ldm + nb;
+        if (full && vec_mask) {
+          uint4 mw[2];
+          mw[0] = *reinterpret_cast<const uint4 *>(mk);
+          mw[1] = *reinterpret_cast<const uint4 *>(mk + 8);
+          const __nv_bfloat16 *mb = reinterpret_cast<const __nv_bfloat16 *>(mw);
+#pragma unroll
+          for (int e = 0; e < 16; ++e) x[e] = __bfloat162float(mb[e]) > 0.0f ? x[e] : 0.0f;
+        } else {
+#pragma unroll
+          for (int e = 0; e < 16; ++e)
+            if (nb + e < a.N) x[e] = __bfloat162float(mk[e]) > 0.0f ? x[e] : 0.0f;
         }
       }
+      __nv_bfloat16 *o = static_cast<__nv_bfloat16 *>(a.out) + (size_t)m * a.ldo + nb;
+      if (full && vec_bf16) {
+        uint4 pk[2];
+        uint32_t *pw = reinterpret_cast<uint32_t *>(pk);
+#pragma unroll
+        for (int e = 0; e < 16; e += 2) {
+          const __nv_bfloat162 b2 = __floats2bfloat162_rn(x[e], x[e + 1]);
+          pw[e / 2] = *reinterpret_cast<const uint32_t *>(&b2);
+        }
+        *reinterpret_cast<uint4 *>(o) = pk[0];
+        *reinterpret_cast<uint4 *>(o + 8) = pk[1];
+      } else {
+#pragma unroll
+        for (int e = 0; e < 16; ++e)
+          if (nb + e < a.N) o[e] = __float2bfloat16_rn(x[e]);
+      }
     }
+    __syncwarp();
     if (!ok && lane == 0) atomicOr(a.status, SF_DEVERR_TIMEOUT_EPILOGUE);
   }
   tc_fence_before();
