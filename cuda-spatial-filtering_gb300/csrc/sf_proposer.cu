@@ -95,9 +95,9 @@ __global__ void sf_proposer_features_kernel(const int32_t *vis, int R, int NBL, 
   for (int k = 2 * NBL + threadIdx.x; k < ldx; k += blockDim.x) xr[k] = __float2bfloat16_rn(0.0f);
 }
 
-// bytes of one warp's region: A n x (n + 1), U and V 4 n, W0 B n, factors n (float2), s n (float)
+// bytes of one warp's region: A n x (n + 1), U and V 4 n, W0 B n, factors n (float2), s and 1 / s n (float)
 __host__ __device__ inline size_t rr_region(int n, int B) {
-  const size_t per = ((size_t)n * (n + 1) + 2 * (size_t)KV * n + (size_t)B * n + (size_t)n) * 8 + (size_t)n * 4;
+  const size_t per = ((size_t)n * (n + 1) + 2 * (size_t)KV * n + (size_t)B * n + (size_t)n) * 8 + 2 * (size_t)n * 4;
   return (per + 15) & ~size_t(15);
 }
 
@@ -136,6 +136,7 @@ __global__ void __launch_bounds__(128) sf_rr_kernel(const RRArgs a) {
   float2 *W0 = V + KV * n;
   float2 *fac = W0 + B * n;
   float *s = reinterpret_cast<float *>(fac + n);
+  float *rsd = s + n;  // 1 / s
   // same-pol entry (p, p) of baseline b at vin[8 b], vin[8 b + 1] (layout [b][Pol][Pol][2])
   const int32_t *vin = a.vis + (size_t)c * a.NBL * 8 + 6 * p;
   const float2 *dp = a.factors + (size_t)row * n;
@@ -145,7 +146,9 @@ __global__ void __launch_bounds__(128) sf_rr_kernel(const RRArgs a) {
   for (int i = lane; i < n; i += 32) {
     const float2 d = dp[i];
     fac[i] = d;
-    s[i] = sqrtf(fmaxf(static_cast<float>(vin[(size_t)baseline_of(i, i) * 8]) * (d.x * d.x + d.y * d.y), 1e-10f));
+    const float sq = fmaxf(static_cast<float>(vin[(size_t)baseline_of(i, i) * 8]) * (d.x * d.x + d.y * d.y), 1e-10f);
+    s[i] = sqrtf(sq);
+    rsd[i] = rsqrtf(sq);
   }
   __syncwarp();
   {
@@ -161,13 +164,15 @@ __global__ void __launch_bounds__(128) sf_rr_kernel(const RRArgs a) {
       for (int u = 0; u < 8; ++u) {
         const int b = b0 + u * 32 + lane;
         if (b < nb) {
-          int j = static_cast<int>((sqrtf(8.0f * static_cast<float>(b) + 1.0f) - 1.0f) * 0.5f);
+          // b = j (j + 1) / 2 + i: j from an approximate square root, then corrected exactly
+          const float t8 = 8.0f * static_cast<float>(b) + 1.0f;
+          int j = static_cast<int>((t8 * rsqrtf(t8) - 1.0f) * 0.5f);
           if ((j + 1) * (j + 2) / 2 <= b) ++j;
           if (j * (j + 1) / 2 > b) --j;
           const int i = b - j * (j + 1) / 2;
           float2 x = make_float2(static_cast<float>(raw[u].x), static_cast<float>(raw[u].y));
           x = cmulc(cmul(fac[i], x), fac[j]);  // d_i V(i, j) conj(d_j), element (i, j)
-          const float inv = 1.0f / (s[i] * s[j]);
+          const float inv = rsd[i] * rsd[j];
           A[i * ld + j] = i == j ? make_float2(x.x * inv, 0.0f) : make_float2(x.x * inv, x.y * inv);
           if (j > i) A[j * ld + i] = make_float2(x.x * inv, -x.y * inv);
         }
@@ -395,7 +400,7 @@ __global__ void __launch_bounds__(128) sf_rr_kernel(const RRArgs a) {
       for (int l = 0; l < KV; ++l)
         if (l != k) off += H[k][l].x * H[k][l].x + H[k][l].y * H[k][l].y;
     }
-    if (off <= 1e-14f * diag * diag + 1e-30f) break;
+    if (off <= 1e-10f * diag * diag + 1e-30f) break;  // residuals are tested at 1e-3 theta_0
 #pragma unroll
     for (int pp = 0; pp < KV - 1; ++pp)
 #pragma unroll
