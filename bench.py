@@ -98,7 +98,7 @@ def run_stage_only(args):
     plan.correlate(d_s[0], d_sc[0], sfgb.SF_WINDOW_ALIGNED, vis, stream=stream)
     name = {"corr": "sf_corr_kernel", "eig": "sf_eig_kernel", "beam": "sf_beam_kernel",
             "packet_spectra": "sf_packet_spectra_kernel",
-            "beam_spectra": "sf_beam_spectra_kernel"}[args.only_stage]
+            "beam_spectra": "sf_beam_spectra_kernel", "learned_eig": "sf_learned_eig"}[args.only_stage]
     res = _stage_breakdown(plan, d_s, d_sc, vis, ev, cnt, beams, stream, args.steps, only=name)
     rc, bits = plan.status(stream)
     if rc != 0:
@@ -972,6 +972,14 @@ def _stage_breakdown(plan, d_s, d_sc, vis, ev, cnt, beams, stream, reps, only=No
         "sf_packet_spectra_kernel": lambda i: plan.packet_spectra(beams, 2 * B, TRIM, spec_pk, stream=stream),
         "sf_beam_spectra_kernel": lambda i: plan.beam_spectra(beams, 2 * B, DOWNSAMPLE, spec_bs, stream=stream),
     }
+    if only == "sf_learned_eig":
+        # the learned eigen stage (features, MLP, Rayleigh-Ritz, fallback) with an untrained
+        # proposer: the refinement does the same work whatever the model's quality
+        from sfgb import proposer as prop
+        q = prop.Proposer(R, 512, 2 * C)
+        q.init_params(seed=0)
+        stages["sf_learned_eig"] = lambda i: plan.covariance_eig_learned(q, vis, sfgb.SF_K_FIXED, 0.0, 3, 1e-3,
+                                                                         counts=cnt, stream=stream)
     spec_pk = torch.empty(plan.packet_spectra_shape(2 * B, TRIM), dtype=torch.float32, device=beams.device)
     spec_bs = torch.empty(plan.beam_spectra_shape(2 * B, DOWNSAMPLE), dtype=torch.float32, device=beams.device)
     out = {}
@@ -1147,7 +1155,7 @@ def main():
     ap.add_argument("--learned-epochs", type=int, default=12)
     ap.add_argument("--channels", type=int, default=C,
                     help="channels per integration (default: the 384-channel workload)")
-    ap.add_argument("--only-stage", choices=["corr", "eig", "beam", "packet_spectra", "beam_spectra"],
+    ap.add_argument("--only-stage", choices=["corr", "eig", "beam", "packet_spectra", "beam_spectra", "learned_eig"],
                     help="launch one stage kernel only (for a profiler capture)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

@@ -1,9 +1,8 @@
 """Generate golden vectors from the reference's own Python implementation.
 
-Run in a container that has the reference checkout (its path is given by
-SF_REFERENCE_ROOT, default /root/reference):
+Run where a reference checkout exists, with its path in SF_REFERENCE_ROOT:
 
-    python tests/golden/make_golden.py
+    SF_REFERENCE_ROOT=/path/to/cuda-spatial-filtering python tests/golden/make_golden.py
 
 It imports ``scripts/adaptive_detection_reference.py`` from the reference
 (detect_k, build_null_projection, build_shrink_projection,
@@ -24,7 +23,9 @@ HERE = Path(__file__).resolve().parent
 
 
 def load_reference_module():
-    root = Path(os.environ.get("SF_REFERENCE_ROOT", "/root/reference"))
+    if not os.environ.get("SF_REFERENCE_ROOT"):
+        raise SystemExit("set SF_REFERENCE_ROOT to the reference checkout")
+    root = Path(os.environ["SF_REFERENCE_ROOT"])
     path = root / "scripts" / "adaptive_detection_reference.py"
     spec = importlib.util.spec_from_file_location("adaptive_detection_reference", path)
     mod = importlib.util.module_from_spec(spec)
