@@ -63,6 +63,21 @@ struct SmallEigArgs {
   // matrices list[0 .. *list_count) instead of all 2C (the learned chain's fallback), or NULL
   const int32_t *list;
   const int32_t *list_count;
+  // batched form: matrices items[first_item .. first_item + n_items) (R = their largest n), or NULL
+  const SfEigItem *items;
+  int first_item, n_items;
+};
+
+// one matrix's inputs and outputs
+struct SmallMat {
+  int n;
+  const int32_t *vin;   // same-pol entry (p, p) of packed baseline b at vin[8 b], vin[8 b + 1]
+  const float2 *fac;    // receiver factors [n], or NULL for unit factors
+  const __half2 *w;     // weights [B][n]
+  float2 *we;           // effective weights [2B][n] (slot 0 original, slot 1 projected)
+  float *ev;            // eigenvalues [n], or NULL
+  int32_t *cnt;         // K, or NULL
+  int kfix;             // K of the fixed rule (clamped to [0, n] here)
 };
 
 // leading dimension (float2) of the matrix: the smallest ld >= n with ld = 4 (mod 16)
@@ -237,12 +252,11 @@ __device__ __forceinline__ float2 rank2(float2 r, const float4 &qi, const float4
   return r;
 }
 
-// the whole solve of matrix bt (c * 2 + p) by the CTA
-__device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, int bt, uint8_t *smem) {
+// the whole solve of one matrix by the CTA
+__device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, const SmallMat &mt, uint8_t *smem) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int rs = tid >> 2, sg = tid & 3;  // row slot, column segment
-  const int n = a.R, B = a.B, ld = small_ld(n);
-  const int c = bt >> 1, p = bt & 1;
+  const int n = mt.n, B = a.B, ld = small_ld(n);
   const SRegion L = s_region(n, B);
   float4 *vp = reinterpret_cast<float4 *>(smem + L.vp);
   float2 *de = reinterpret_cast<float2 *>(smem + L.de);
@@ -268,17 +282,17 @@ __device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, int bt, uin
   float *sd = lam + n;
   int *cnt = reinterpret_cast<int *>(smem + L.cnt);
   // same-pol entry (p, p) of baseline b at vin[8 b], vin[8 b + 1] (layout [b][Pol][Pol][2])
-  const int32_t *vin = a.vis + (size_t)c * a.NBL * 8 + 6 * p;
+  const int32_t *vin = mt.vin;
 
   // ---- 1. covariance d_i V conj(d_j), both triangles, whitened ----
   for (int i = tid; i < n; i += NT) {
-    const float2 di = a.factors[(size_t)bt * n + i];
+    const float2 di = mt.fac ? mt.fac[i] : make_float2(1.0f, 0.0f);
     fac[i] = di;
     const float v = static_cast<float>(vin[(size_t)baseline_of(i, i) * 8]);
     sd[i] = sqrtf(fmaxf(v * (di.x * di.x + di.y * di.y), 1e-10f));
   }
   {
-    const __half2 *w = a.weights + (size_t)bt * B * n;
+    const __half2 *w = mt.w;
     for (int ee = tid; ee < B * n; ee += NT) {
       const float2 x = __half22float2(w[ee]);
       W0[ee] = x;
@@ -466,8 +480,8 @@ __device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, int bt, uin
   }
   __syncthreads();
   const float glo = redf[8], ghi = redf[9], atol = redf[10], pivs = redf[11], unsc = redf[12], pert = redf[13];
-  const int Kfix = max(0, min(n, a.fixed_counts ? a.fixed_counts[c] : 0));
-  const bool need_all = a.k_rule != SF_K_FIXED || a.evals != nullptr || a.shrink || Kfix > 32;
+  const int Kfix = max(0, min(n, mt.kfix));
+  const bool need_all = a.k_rule != SF_K_FIXED || mt.ev != nullptr || a.shrink || Kfix > 32;
   {
     float xs[4];
     int cn[4];
@@ -528,8 +542,8 @@ __device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, int bt, uin
     if (mine && sub == 0) lam[j] = 0.5f * (lo + hi) * unsc;
   }
   __syncthreads();
-  if (a.evals)
-    for (int j = tid; j < n; j += NT) a.evals[(size_t)bt * n + j] = lam[j];
+  if (mt.ev)
+    for (int j = tid; j < n; j += NT) mt.ev[j] = lam[j];
 
   // ---- 4. K ----
   int *sK = reinterpret_cast<int *>(redf + 14);
@@ -547,7 +561,7 @@ __device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, int bt, uin
     }
     K = max(0, min(n, K));
     *sK = K;
-    if (a.counts) a.counts[bt] = K;
+    if (mt.cnt) *mt.cnt = K;
   }
   __syncthreads();
   const int K = *sK;
@@ -765,7 +779,7 @@ __device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, int bt, uin
     }
     __syncthreads();
   }
-  float2 *we = a.weff + (size_t)bt * 2 * B * n;
+  float2 *we = mt.we;
   for (int ee = tid; ee < B * n; ee += NT) {
     const int col = ee - (ee / n) * n;
     we[ee] = cmul(W0[ee], fac[col]);
@@ -773,13 +787,36 @@ __device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, int bt, uin
   }
 }
 
-// One CTA per matrix, or in list mode a grid of at most one resident wave
-// walking list[0 .. *list_count) (the count is known only on the device)
+// One CTA per matrix, or a grid of at most one resident wave walking the
+// device list (its count is known only on the device) or the item range
 __global__ void __launch_bounds__(NT, 6) sf_eig_small_kernel(const SmallEigArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
-  const int count = a.list ? *a.list_count : 2 * a.C;
+  const int count = a.list ? *a.list_count : (a.items ? a.n_items : 2 * a.C);
   for (int slot = blockIdx.x; slot < count; slot += gridDim.x) {
-    eig_small_one(a, a.list ? a.list[slot] : slot, smem);
+    SmallMat mt;
+    if (a.items) {
+      const SfEigItem it = a.items[a.first_item + slot];
+      mt.n = it.n;
+      mt.vin = a.vis + it.vis_off + 6 * it.pol;
+      mt.fac = a.factors ? a.factors + it.factor_off : nullptr;
+      mt.w = a.weights + it.weight_off;
+      mt.we = a.weff + it.weff_off;
+      mt.ev = a.evals ? a.evals + it.eval_off : nullptr;
+      mt.cnt = a.counts ? a.counts + it.count_idx : nullptr;
+      mt.kfix = a.fixed_counts ? a.fixed_counts[it.count_idx] : 0;
+    } else {
+      const int bt = a.list ? a.list[slot] : slot;  // c * 2 + p
+      const int c = bt >> 1, n = a.R;
+      mt.n = n;
+      mt.vin = a.vis + (size_t)c * a.NBL * 8 + 6 * (bt & 1);
+      mt.fac = a.factors + (size_t)bt * n;
+      mt.w = a.weights + (size_t)bt * a.B * n;
+      mt.we = a.weff + (size_t)bt * 2 * a.B * n;
+      mt.ev = a.evals ? a.evals + (size_t)bt * n : nullptr;
+      mt.cnt = a.counts ? a.counts + bt : nullptr;
+      mt.kfix = a.fixed_counts ? a.fixed_counts[c] : 0;
+    }
+    eig_small_one(a, mt, smem);
     __syncthreads();  // the next matrix reuses the shared memory
   }
 }
@@ -811,6 +848,9 @@ cudaError_t sf_launch_eig_small(const sf_plan *p, const int32_t *vis, int k_rule
   a.k_rule = k_rule;
   a.shrink = shrink;
   a.delta = delta;
+  a.items = nullptr;
+  a.first_item = 0;
+  a.n_items = 0;
   const size_t smem = s_region(p->R, p->B).total;
   cudaError_t e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_small_kernel), smem);
   if (e != cudaSuccess) return e;
@@ -821,6 +861,48 @@ cudaError_t sf_launch_eig_small(const sf_plan *p, const int32_t *vis, int k_rule
     if (e != cudaSuccess) return e;
     grid = std::min(grid, std::max(1, per_sm) * p->num_sms);
   }
+  sf_eig_small_kernel<<<grid, NT, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
+int sf_eig_small_items_supported(int n_max, int B) {
+  return n_max >= 2 && n_max <= SN_MAX && B <= SB_MAX && s_region(n_max, B).total <= (size_t)sf_device_max_smem();
+}
+
+cudaError_t sf_launch_eig_small_items(const SfEigItem *items, int first, int count, int n_max, int B,
+                                      const int32_t *vis, const float2 *factors, const __half2 *weights,
+                                      const int32_t *fixed_counts, int k_rule, float delta, int shrink,
+                                      float *evals, int32_t *counts, float2 *weff, int num_sms,
+                                      cudaStream_t stream) {
+  if (count <= 0) return cudaSuccess;
+  if (!sf_eig_small_items_supported(n_max, B)) return cudaErrorInvalidValue;
+  SmallEigArgs a;
+  a.vis = vis;
+  a.factors = factors;
+  a.weights = weights;
+  a.fixed_counts = fixed_counts;
+  a.evals = evals;
+  a.counts = counts;
+  a.weff = weff;
+  a.C = 0;
+  a.R = n_max;
+  a.B = B;
+  a.NBL = 0;
+  a.k_rule = k_rule;
+  a.shrink = shrink;
+  a.delta = delta;
+  a.list = nullptr;
+  a.list_count = nullptr;
+  a.items = items;
+  a.first_item = first;
+  a.n_items = count;
+  const size_t smem = s_region(n_max, B).total;
+  cudaError_t e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_small_kernel), smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sf_eig_small_kernel, NT, smem);
+  if (e != cudaSuccess) return e;
+  const int grid = std::min(count, std::max(1, per_sm) * num_sms);
   sf_eig_small_kernel<<<grid, NT, smem, stream>>>(a);
   return cudaGetLastError();
 }
