@@ -474,13 +474,13 @@ int sf_batch_covariance_eig(sf_batch *b, const int32_t *d_vis, int32_t k_rule, f
       BT_TRY(sf_batch_launch_scales(b->L, b->n_units, b->d_weff, b->d_scales, s), "beam scales");
     return SF_OK;
   }
-  // classes up to 64 receivers: four warps per matrix (sf_eig_small.cu); 128: one CTA per matrix
+  // size classes up to 128 receivers: sf_eig_small.cu (four or sixteen warps per matrix)
   auto launch = [&](int g, cudaStream_t st) {
     const int first = b->eig_first[g], count = b->eig_first[g + 1] - b->eig_first[g];
     if (sf_eig_small_items_supported(b->eig_nmax[g], b->B))
       return sf_launch_eig_small_items(b->d_eig_items, first, count, b->eig_nmax[g], b->B, d_vis, nullptr,
                                        b->d_weights, b->d_fixed, k_rule, delta, shrink ? 1 : 0, d_evals, d_counts,
-                                       b->d_weff, b->num_sms, st);
+                                       b->d_weff, b->d_status, b->num_sms, st);
     return sf_launch_eig_topk_items(b->d_eig_items, first, count, b->eig_nmax[g], b->B, d_vis, nullptr,
                                     b->d_weights, b->d_fixed, k_rule, delta, shrink ? 1 : 0, d_evals, d_counts,
                                     b->d_weff, b->d_status, st);

@@ -393,7 +393,7 @@ cudaError_t sf_launch_eig(const sf_plan *p, const int32_t *vis, int eig_mode, in
                           __half2 *proj, cudaStream_t stream) {
   // The adaptive path needs only eigenvalues and the top-K eigenvectors:
   // the tridiagonal solvers serve it unless every eigenvector (or the
-  // projector itself) is asked for -- sf_eig_small.cu up to 64 receivers and
+  // projector itself) is asked for -- sf_eig_small.cu up to 128 receivers and
   // 16 beams, else sf_eig_topk.cu.
   if (eig_mode == SF_EIG_SAME_POL_WHITENED && evecs == nullptr && proj == nullptr) {
     if (sf_eig_small_supported(p))

@@ -1,5 +1,6 @@
-// Adaptive-path eigensolver for up to 64 receivers and 16 beams: one CTA of
-// four warps per (channel, pol) covariance.  Same algorithm as
+// Adaptive-path eigensolver for up to 128 receivers and 16 beams: one CTA per
+// (channel, pol) covariance -- four warps with two rows per lane up to 64
+// receivers, sixteen warps with four rows per lane up to 128.  Same algorithm as
 // sf_eig_topk.cu -- whitening, Householder tridiagonalisation, Sturm counts
 // with multisection, K, inverse iteration for the top K, back-transform,
 // un-whitening, projected weights -- laid out so that no thread walks a long
@@ -9,7 +10,7 @@
 //   (columns j = s mod 4), so a thread touches about m / 4 elements per
 //   step, with its shared-memory loads issued in batches of four.  Warp 0
 //   updates column 0 of the trailing matrix in registers and forms the next
-//   reflector from them while warps 1-3 do the rest of the rank-2 update, so
+//   reflector from them while the other warps do the rest of the rank-2 update, so
 //   a step costs two CTA barriers (after tau A v, after the update).  The scaled reflector
 //   is kept in the dead upper triangle (row k), where the back-transform
 //   reads it with unit stride.
@@ -39,15 +40,17 @@
 
 namespace {
 
-constexpr int SN_MAX = 64;
+constexpr int SN_MAX = 128;
 constexpr int SB_MAX = 16;
-constexpr int NT = 128;             // threads per matrix
-constexpr int NWARP = NT / 32;
 constexpr int S_GROUP = 8;          // inverse-iteration vectors per pass (lanes 0..7 of warp 0)
 constexpr int S_INV_ITERS = 3;
-constexpr int S_COARSE = 4 * NT;    // coarse Sturm grid points
-constexpr int S_VEC = NWARP;        // eigenvectors back-transformed per pass (one per warp)
+constexpr int S_COARSE = 512;       // coarse Sturm grid points (four per thread of the first 128)
+constexpr int S_VEC = 4;            // eigenvectors back-transformed per pass (one per warp of warps 0-3)
+constexpr int S_RED = 32;           // float2 slots of the cross-warp partials (16 warps) and scalars
 constexpr unsigned FULL = 0xffffffffu;
+
+// top-K eigenvectors of T kept in shared memory: every one up to 64 receivers, 32 beyond
+__host__ __device__ inline int small_xk(int n) { return n <= 64 ? n : 32; }
 
 struct SmallEigArgs {
   const int32_t *vis;
@@ -57,6 +60,7 @@ struct SmallEigArgs {
   float *evals;
   int32_t *counts;
   float2 *weff;
+  uint32_t *status;  // SF_DEVERR_BAD_SHAPE when K exceeds the kept eigenvectors (K is clamped)
   int C, R, B, NBL;
   int k_rule, shrink;
   float delta;
@@ -99,8 +103,8 @@ __host__ __device__ inline SRegion s_region(int n, int B) {
   r.Wp = o;    o += 8 * (size_t)B * n;
   r.Z = o;     o += 8 * (size_t)S_VEC * n;
   r.coef = o;  o += 8 * (size_t)S_VEC * SB_MAX;
-  r.red = o;   o += 8 * 16;                         // cross-warp partials and scalars
-  r.X = o;     o += 4 * (size_t)n * n;              // float: top-K eigenvectors of T
+  r.red = o;   o += 8 * (size_t)S_RED;               // cross-warp partials and scalars
+  r.X = o;     o += 4 * (size_t)small_xk(n) * n;    // float: top-K eigenvectors of T
   r.LU = o;    o += 4 * 5 * (size_t)S_GROUP * n;    // float: inverse-iteration factors
   r.dvec = o;  o += 4 * 5 * (size_t)n;              // float: d, e, e2, lam, sd
   r.cnt = o;   o += 4 * (size_t)S_COARSE;           // int: coarse-grid counts
@@ -201,19 +205,27 @@ __device__ __forceinline__ float grid_point(float lo, float hi, int P, int npts)
 }
 
 // Warp-wide: the reflector of column kk (zlarfg) from values in registers:
-// lane l holds rows kk + l (r0) and kk + 32 + l (r1) of the column, so the
-// entries c_i = A[kk+1+i][kk], i < mm = n - kk - 1, are r0 of lane i + 1 and
-// r1 of lane i - 31.  H^H c = beta e_1 with H = I - tau v v^H, v_0 = 1.
-// Writes v to vb[i].xy (i < mm), the scaled entries v_i (i >= 1) into the dead
-// upper triangle A[kk][kk+1+i], taus[kk] and e[kk] = beta.
-__device__ __forceinline__ void make_reflector(float2 r0, float2 r1, float2 *A, int ld, int n, int kk, float4 *vb,
+// lane l holds rows kk + l + 32 q (r[q], q < NPL) of the column, so the
+// entries c_i = A[kk+1+i][kk], i < mm = n - kk - 1, are r[q] of lane i + 1 - 32 q.
+// H^H c = beta e_1 with H = I - tau v v^H, v_0 = 1.  Writes v to vb[i].xy
+// (i < mm), the scaled entries v_i (i >= 1) into the dead upper triangle
+// A[kk][kk+1+i], taus[kk] and e[kk] = beta.
+template <int NPL>
+__device__ __forceinline__ void make_reflector(const float2 (&r)[NPL], float2 *A, int ld, int n, int kk, float4 *vb,
                                                float2 *taus, float *e, int lane) {
   const int mm = n - kk - 1;
-  const bool h0 = lane >= 2 && lane <= mm, h1 = lane + 32 <= mm;
-  const float2 alpha = make_float2(__shfl_sync(FULL, r0.x, 1), __shfl_sync(FULL, r0.y, 1));
-  float2 c0 = h0 ? r0 : make_float2(0.0f, 0.0f);
-  float2 c1 = h1 ? r1 : make_float2(0.0f, 0.0f);
-  const float xnorm2 = wsum(c0.x * c0.x + c0.y * c0.y + c1.x * c1.x + c1.y * c1.y);
+  const float2 alpha = make_float2(__shfl_sync(FULL, r[0].x, 1), __shfl_sync(FULL, r[0].y, 1));
+  float2 c[NPL];
+  bool h[NPL];
+  float part = 0.0f;
+#pragma unroll
+  for (int q = 0; q < NPL; ++q) {
+    const int row = lane + 32 * q;  // entry row - 1
+    h[q] = row >= 2 && row <= mm;
+    c[q] = h[q] ? r[q] : make_float2(0.0f, 0.0f);
+    part += c[q].x * c[q].x + c[q].y * c[q].y;
+  }
+  const float xnorm2 = wsum(part);
   float2 tau = make_float2(0.0f, 0.0f);
   float beta = alpha.x;
   if (!(xnorm2 == 0.0f && alpha.y == 0.0f)) {
@@ -225,17 +237,17 @@ __device__ __forceinline__ void make_reflector(float2 r0, float2 r1, float2 *A, 
     const float2 am = make_float2(alpha.x - beta, alpha.y);  // |am| >= nrm > 0
     const float inv = fast_rcp(am.x * am.x + am.y * am.y);
     const float2 sc = make_float2(am.x * inv, -am.y * inv);
-    c0 = cmul(c0, sc);
-    c1 = cmul(c1, sc);
+#pragma unroll
+    for (int q = 0; q < NPL; ++q) c[q] = cmul(c[q], sc);
   }
   float2 *urow = A + (size_t)kk * ld + (kk + 1);  // entry i at urow[i]
-  if (h0) {
-    *reinterpret_cast<float2 *>(&vb[lane - 1]) = c0;
-    urow[lane - 1] = c0;
-  }
-  if (h1) {
-    *reinterpret_cast<float2 *>(&vb[lane + 31]) = c1;
-    urow[lane + 31] = c1;
+#pragma unroll
+  for (int q = 0; q < NPL; ++q) {
+    if (h[q]) {
+      const int i = lane + 32 * q - 1;
+      *reinterpret_cast<float2 *>(&vb[i]) = c[q];
+      urow[i] = c[q];
+    }
   }
   if (lane == 0) {
     *reinterpret_cast<float2 *>(&vb[0]) = make_float2(1.0f, 0.0f);
@@ -252,8 +264,11 @@ __device__ __forceinline__ float2 rank2(float2 r, const float4 &qi, const float4
   return r;
 }
 
-// the whole solve of one matrix by the CTA
+// the whole solve of one matrix by the CTA of NT threads, NPL rows per lane (n <= 32 NPL)
+template <int NT, int NPL>
 __device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, const SmallMat &mt, uint8_t *smem) {
+  constexpr int NWARP = NT / 32;
+  constexpr int RS = NT / 4;  // row slots of the row-split loops (four lanes per row)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int rs = tid >> 2, sg = tid & 3;  // row slot, column segment
   const int n = mt.n, B = a.B, ld = small_ld(n);
@@ -331,9 +346,10 @@ __device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, const Small
 
   // ---- 2. Householder tridiagonalisation T = Q^H A Q (lower) ----
   if (warp == 0) {
-    const float2 r0 = lane < n ? A[(size_t)lane * ld] : make_float2(0.0f, 0.0f);
-    const float2 r1 = lane + 32 < n ? A[(size_t)(lane + 32) * ld] : make_float2(0.0f, 0.0f);
-    make_reflector(r0, r1, A, ld, n, 0, vp, taus, e, lane);
+    float2 r[NPL];
+#pragma unroll
+    for (int q = 0; q < NPL; ++q) r[q] = lane + 32 * q < n ? A[(size_t)(lane + 32 * q) * ld] : make_float2(0.0f, 0.0f);
+    make_reflector<NPL>(r, A, ld, n, 0, vp, taus, e, lane);
   }
   __syncthreads();
   for (int k = 0; k < n - 1; ++k) {
@@ -345,11 +361,10 @@ __device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, const Small
     float2 *A22 = A + (size_t)(k + 1) * ld + (k + 1);
     float cvv = 0.0f;
     if (act) {
-      // p = tau A22 v: thread (rs, sg) sums the columns j = sg (mod 4) of rows rs, rs + 32
+      // p = tau A22 v: thread (rs, sg) sums the columns j = sg (mod 4) of rows rs, rs + RS, ...
       float pr = 0.0f, pim = 0.0f;  // this thread's part of p^H v
-      for (int q = 0; q < 2; ++q) {
-        if (32 * q >= m) break;  // uniform
-        const int i = rs + 32 * q;
+      for (int q = 0; RS * q < m; ++q) {  // uniform
+        const int i = rs + RS * q;
         const int jm = i < m ? m : 0;
         const float2 *row = A22 + (size_t)i * ld;
         const float2 vi = sg == 0 && i < m ? vpart(vb[i]) : make_float2(0.0f, 0.0f);
@@ -405,21 +420,23 @@ __device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, const Small
       cvv = -(tau.x * pv.x - tau.y * pv.y);
     }
     if (warp == 0) {
-      // column 0 of A22 (rows lane, lane + 32): the next diagonal entry and the next reflector,
-      // formed while warps 1-3 update the rest
-      float2 r0 = lane < m ? A22[(size_t)lane * ld] : make_float2(0.0f, 0.0f);
-      float2 r1 = lane + 32 < m ? A22[(size_t)(lane + 32) * ld] : make_float2(0.0f, 0.0f);
+      // column 0 of A22 (rows lane + 32 q): the next diagonal entry and the next reflector,
+      // formed while the other warps update the rest
+      float2 r[NPL];
+#pragma unroll
+      for (int q = 0; q < NPL; ++q) r[q] = lane + 32 * q < m ? A22[(size_t)(lane + 32 * q) * ld] : make_float2(0.0f, 0.0f);
       if (act) {
         const float4 q0 = vb[0];
-        if (lane < m) r0 = rank2(r0, vb[lane], q0, cvv);
-        if (lane + 32 < m) r1 = rank2(r1, vb[lane + 32], q0, cvv);
+#pragma unroll
+        for (int q = 0; q < NPL; ++q)
+          if (lane + 32 * q < m) r[q] = rank2(r[q], vb[lane + 32 * q], q0, cvv);
       }
-      if (lane == 0) A22[0] = r0;
-      if (k + 1 < n - 1) make_reflector(r0, r1, A, ld, n, k + 1, vnext, taus, e, lane);
+      if (lane == 0) A22[0] = r[0];
+      if (k + 1 < n - 1) make_reflector<NPL>(r, A, ld, n, k + 1, vnext, taus, e, lane);
     } else if (act) {
-      // rows 1.. and columns 1.. of A22 (row 0 is the dead mirror of column 0): 24 row slots
+      // rows 1.. and columns 1.. of A22 (row 0 is the dead mirror of column 0): RS - 8 row slots
       const int rs3 = rs - 8;
-      for (int i = 1 + rs3; i < m; i += 24) {
+      for (int i = 1 + rs3; i < m; i += RS - 8) {
         float2 *row = A22 + (size_t)i * ld;
         const float4 qi = vb[i];
         int j = 1 + sg;
@@ -470,19 +487,19 @@ __device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, const Small
     }
     if (lane == 0) {
       const float tn = tnorm * sc, pivs = fmaxf(1e-30f, 1e-30f * emax * sc * sc);
-      redf[8] = glo * sc - (2e-7f * tn + pivs);                  // scaled bracket low
-      redf[9] = ghi * sc + (2e-7f * tn + pivs);                  // scaled bracket high
-      redf[10] = 2.4e-7f * tn + 4.0f * pivs;                     // scaled absolute tolerance
-      redf[11] = pivs;                                           // scaled pivmin
-      redf[12] = __int_as_float((127 + ex) << 23);               // 1 / sc
-      redf[13] = 2.4e-7f * tnorm + fmaxf(1e-30f, 1e-30f * emax);  // inverse-iteration pivot floor
+      redf[40] = glo * sc - (2e-7f * tn + pivs);                  // scaled bracket low
+      redf[41] = ghi * sc + (2e-7f * tn + pivs);                  // scaled bracket high
+      redf[42] = 2.4e-7f * tn + 4.0f * pivs;                     // scaled absolute tolerance
+      redf[43] = pivs;                                           // scaled pivmin
+      redf[44] = __int_as_float((127 + ex) << 23);               // 1 / sc
+      redf[45] = 2.4e-7f * tnorm + fmaxf(1e-30f, 1e-30f * emax);  // inverse-iteration pivot floor
     }
   }
   __syncthreads();
-  const float glo = redf[8], ghi = redf[9], atol = redf[10], pivs = redf[11], unsc = redf[12], pert = redf[13];
+  const float glo = redf[40], ghi = redf[41], atol = redf[42], pivs = redf[43], unsc = redf[44], pert = redf[45];
   const int Kfix = max(0, min(n, mt.kfix));
   const bool need_all = a.k_rule != SF_K_FIXED || mt.ev != nullptr || a.shrink || Kfix > 32;
-  {
+  if (tid < S_COARSE / 4) {
     float xs[4];
     int cn[4];
 #pragma unroll
@@ -546,7 +563,7 @@ __device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, const Small
     for (int j = tid; j < n; j += NT) mt.ev[j] = lam[j];
 
   // ---- 4. K ----
-  int *sK = reinterpret_cast<int *>(redf + 14);
+  int *sK = reinterpret_cast<int *>(redf + 46);
   if (tid == 0) {
     int K = 0;
     if (a.k_rule == SF_K_DETECT) {
@@ -560,6 +577,10 @@ __device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, const Small
       K = Kfix;
     }
     K = max(0, min(n, K));
+    if (K > small_xk(n)) {  // more modes than the kept eigenvectors: null the top ones kept
+      if (a.status) atomicOr(a.status, SF_DEVERR_BAD_SHAPE);
+      K = small_xk(n);
+    }
     *sK = K;
     if (mt.cnt) *mt.cnt = K;
   }
@@ -692,35 +713,46 @@ __device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, const Small
     const int rn = min(S_VEC, K - r0);
     if (warp < rn) {
       const float *x = X + (r0 + warp) * n;
-      float2 z0 = make_float2(lane < n ? x[lane] : 0.0f, 0.0f);
-      float2 z1 = make_float2(lane + 32 < n ? x[lane + 32] : 0.0f, 0.0f);
+      float2 z[NPL];
+#pragma unroll
+      for (int q = 0; q < NPL; ++q) z[q] = make_float2(lane + 32 * q < n ? x[lane + 32 * q] : 0.0f, 0.0f);
       for (int k = n - 2; k >= 0; --k) {
         const float2 tau = taus[k];
         if (tau.x == 0.0f && tau.y == 0.0f) continue;
         // v_(k+1) = 1, v_i = A[k][i] for i > k + 1 (kept in the upper triangle)
-        const int i0 = lane, i1 = lane + 32;
         const float2 *urow = A + (size_t)k * ld;
-        const float2 v0 = i0 > k + 1 && i0 < n ? urow[i0] : make_float2(i0 == k + 1 ? 1.0f : 0.0f, 0.0f);
-        const float2 v1 = i1 > k + 1 && i1 < n ? urow[i1] : make_float2(i1 == k + 1 ? 1.0f : 0.0f, 0.0f);
-        float dre = v0.x * z0.x + v0.y * z0.y + v1.x * z1.x + v1.y * z1.y;  // conj(v) z
-        float dim = v0.x * z0.y - v0.y * z0.x + v1.x * z1.y - v1.y * z1.x;
+        float2 v[NPL];
+        float dre = 0.0f, dim = 0.0f;  // conj(v) z
+#pragma unroll
+        for (int q = 0; q < NPL; ++q) {
+          const int i = lane + 32 * q;
+          v[q] = i > k + 1 && i < n ? urow[i] : make_float2(i == k + 1 ? 1.0f : 0.0f, 0.0f);
+          dre += v[q].x * z[q].x + v[q].y * z[q].y;
+          dim += v[q].x * z[q].y - v[q].y * z[q].x;
+        }
         wsum2(dre, dim);
         const float2 sc = cmul(tau, make_float2(dre, dim));
-        z0 = make_float2(z0.x - (sc.x * v0.x - sc.y * v0.y), z0.y - (sc.x * v0.y + sc.y * v0.x));
-        z1 = make_float2(z1.x - (sc.x * v1.x - sc.y * v1.y), z1.y - (sc.x * v1.y + sc.y * v1.x));
+#pragma unroll
+        for (int q = 0; q < NPL; ++q)
+          z[q] = make_float2(z[q].x - (sc.x * v[q].x - sc.y * v[q].y), z[q].y - (sc.x * v[q].y + sc.y * v[q].x));
       }
       if (!a.shrink) {
         // u = D^1/2 z / |D^1/2 z| (un-whitened, unit norm)
-        const float s0 = lane < n ? sd[lane] : 0.0f, s1 = lane + 32 < n ? sd[lane + 32] : 0.0f;
-        z0 = make_float2(z0.x * s0, z0.y * s0);
-        z1 = make_float2(z1.x * s1, z1.y * s1);
-        const float nrm2 = wsum(z0.x * z0.x + z0.y * z0.y + z1.x * z1.x + z1.y * z1.y);
+        float part = 0.0f;
+#pragma unroll
+        for (int q = 0; q < NPL; ++q) {
+          const float sq = lane + 32 * q < n ? sd[lane + 32 * q] : 0.0f;
+          z[q] = make_float2(z[q].x * sq, z[q].y * sq);
+          part += z[q].x * z[q].x + z[q].y * z[q].y;
+        }
+        const float nrm2 = wsum(part);
         const float inv = nrm2 > 0.0f ? rsqrtf(nrm2) : 0.0f;
-        z0 = make_float2(z0.x * inv, z0.y * inv);
-        z1 = make_float2(z1.x * inv, z1.y * inv);
+#pragma unroll
+        for (int q = 0; q < NPL; ++q) z[q] = make_float2(z[q].x * inv, z[q].y * inv);
       }
-      if (lane < n) Z[warp * n + lane] = z0;
-      if (lane + 32 < n) Z[warp * n + lane + 32] = z1;
+#pragma unroll
+      for (int q = 0; q < NPL; ++q)
+        if (lane + 32 * q < n) Z[warp * n + lane + 32 * q] = z[q];
     }
     __syncthreads();
     // c_(v,m) = wgt_v (W_m . z_v) for the pass's vectors and every beam: g2 lanes per
@@ -789,7 +821,8 @@ __device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, const Small
 
 // One CTA per matrix, or a grid of at most one resident wave walking the
 // device list (its count is known only on the device) or the item range
-__global__ void __launch_bounds__(NT, 6) sf_eig_small_kernel(const SmallEigArgs a) {
+template <int NT, int NPL>
+__global__ void __launch_bounds__(NT, NT == 128 ? 6 : 1) sf_eig_small_kernel(const SmallEigArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   const int count = a.list ? *a.list_count : (a.items ? a.n_items : 2 * a.C);
   for (int slot = blockIdx.x; slot < count; slot += gridDim.x) {
@@ -816,17 +849,54 @@ __global__ void __launch_bounds__(NT, 6) sf_eig_small_kernel(const SmallEigArgs 
       mt.cnt = a.counts ? a.counts + bt : nullptr;
       mt.kfix = a.fixed_counts ? a.fixed_counts[c] : 0;
     }
-    eig_small_one(a, mt, smem);
+    eig_small_one<NT, NPL>(a, mt, smem);
     __syncthreads();  // the next matrix reuses the shared memory
   }
 }
 
 }  // namespace
 
-int sf_eig_small_supported(const sf_plan *p) {
-  return p->R >= 2 && p->R <= SN_MAX && p->B <= SB_MAX &&
-         s_region(p->R, p->B).total <= (size_t)sf_device_max_smem();
+namespace {
+
+// the configuration for matrices of at most n_max receivers: four warps and two rows per lane up
+// to 64, sixteen warps and four rows per lane up to 128
+struct SmallLaunch {
+  const void *fn;
+  int nt;
+};
+SmallLaunch small_config(int n_max) {
+  if (n_max <= 64) return {reinterpret_cast<const void *>(sf_eig_small_kernel<128, 2>), 128};
+  return {reinterpret_cast<const void *>(sf_eig_small_kernel<512, 4>), 512};
 }
+
+bool small_fits(int n_max, int B) {
+  return n_max >= 2 && n_max <= SN_MAX && B <= SB_MAX && s_region(n_max, B).total <= (size_t)sf_device_max_smem();
+}
+
+// grid: every matrix its own CTA (count_hint > 0 and no cap), or at most one resident wave
+cudaError_t launch_small(const SmallEigArgs &a, int n_max, int count, bool one_wave, int num_sms, cudaStream_t stream) {
+  const SmallLaunch cfg = small_config(n_max);
+  const size_t smem = s_region(n_max, a.B).total;
+  cudaError_t e = sf_smem_optin(cfg.fn, smem);
+  if (e != cudaSuccess) return e;
+  int grid = count;
+  if (one_wave) {
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cfg.fn, cfg.nt, smem);
+    if (e != cudaSuccess) return e;
+    grid = std::min(count, std::max(1, per_sm) * num_sms);
+  }
+  if (grid <= 0) return cudaSuccess;
+  if (cfg.nt == 128)
+    sf_eig_small_kernel<128, 2><<<grid, 128, smem, stream>>>(a);
+  else
+    sf_eig_small_kernel<512, 4><<<grid, 512, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+int sf_eig_small_supported(const sf_plan *p) { return small_fits(p->R, p->B); }
 
 cudaError_t sf_launch_eig_small(const sf_plan *p, const int32_t *vis, int k_rule, float delta, int shrink,
                                 float *evals, int32_t *counts, const int32_t *list, const int32_t *list_count,
@@ -841,6 +911,7 @@ cudaError_t sf_launch_eig_small(const sf_plan *p, const int32_t *vis, int k_rule
   a.evals = evals;
   a.counts = counts;
   a.weff = p->d_weff;
+  a.status = p->d_status;
   a.C = p->C;
   a.R = p->R;
   a.B = p->B;
@@ -851,31 +922,19 @@ cudaError_t sf_launch_eig_small(const sf_plan *p, const int32_t *vis, int k_rule
   a.items = nullptr;
   a.first_item = 0;
   a.n_items = 0;
-  const size_t smem = s_region(p->R, p->B).total;
-  cudaError_t e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_small_kernel), smem);
-  if (e != cudaSuccess) return e;
-  int grid = 2 * p->C;
-  if (list) {
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sf_eig_small_kernel, NT, smem);
-    if (e != cudaSuccess) return e;
-    grid = std::min(grid, std::max(1, per_sm) * p->num_sms);
-  }
-  sf_eig_small_kernel<<<grid, NT, smem, stream>>>(a);
-  return cudaGetLastError();
+  // one CTA per matrix; the device list (whose count only the device knows) by one resident wave
+  return launch_small(a, p->R, 2 * p->C, list != nullptr, p->num_sms, stream);
 }
 
-int sf_eig_small_items_supported(int n_max, int B) {
-  return n_max >= 2 && n_max <= SN_MAX && B <= SB_MAX && s_region(n_max, B).total <= (size_t)sf_device_max_smem();
-}
+int sf_eig_small_items_supported(int n_max, int B) { return small_fits(n_max, B); }
 
 cudaError_t sf_launch_eig_small_items(const SfEigItem *items, int first, int count, int n_max, int B,
                                       const int32_t *vis, const float2 *factors, const __half2 *weights,
                                       const int32_t *fixed_counts, int k_rule, float delta, int shrink,
-                                      float *evals, int32_t *counts, float2 *weff, int num_sms,
+                                      float *evals, int32_t *counts, float2 *weff, uint32_t *status, int num_sms,
                                       cudaStream_t stream) {
   if (count <= 0) return cudaSuccess;
-  if (!sf_eig_small_items_supported(n_max, B)) return cudaErrorInvalidValue;
+  if (!small_fits(n_max, B)) return cudaErrorInvalidValue;
   SmallEigArgs a;
   a.vis = vis;
   a.factors = factors;
@@ -884,6 +943,7 @@ cudaError_t sf_launch_eig_small_items(const SfEigItem *items, int first, int cou
   a.evals = evals;
   a.counts = counts;
   a.weff = weff;
+  a.status = status;
   a.C = 0;
   a.R = n_max;
   a.B = B;
@@ -896,13 +956,5 @@ cudaError_t sf_launch_eig_small_items(const SfEigItem *items, int first, int cou
   a.items = items;
   a.first_item = first;
   a.n_items = count;
-  const size_t smem = s_region(n_max, B).total;
-  cudaError_t e = sf_smem_optin(reinterpret_cast<const void *>(sf_eig_small_kernel), smem);
-  if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sf_eig_small_kernel, NT, smem);
-  if (e != cudaSuccess) return e;
-  const int grid = std::min(count, std::max(1, per_sm) * num_sms);
-  sf_eig_small_kernel<<<grid, NT, smem, stream>>>(a);
-  return cudaGetLastError();
+  return launch_small(a, n_max, count, true, num_sms, stream);
 }

@@ -113,8 +113,8 @@ cudaError_t sf_launch_eig_topk_items(const SfEigItem *items, int first, int coun
                                      const int32_t *fixed_counts, int k_rule, float delta, int shrink, float *evals,
                                      int32_t *counts, float2 *weff, uint32_t *status, cudaStream_t stream);
 int sf_eig_topk_supported(const sf_plan *p);
-// One CTA of four warps per (channel, pol) covariance (sf_eig_small.cu):
-// the adaptive path for R <= 64 and B <= 16.  With list != NULL only the
+// One CTA per (channel, pol) covariance (sf_eig_small.cu): the adaptive
+// path for R <= 128 and B <= 16 (four warps up to 64 receivers, sixteen up to 128).  With list != NULL only the
 // matrices list[0 .. *list_count) (count read on the device, at most 2C).
 int sf_eig_small_supported(const sf_plan *p);
 // The batched form's matrices items[first .. first + count) of at most n_max receivers.
@@ -122,7 +122,7 @@ int sf_eig_small_items_supported(int n_max, int B);
 cudaError_t sf_launch_eig_small_items(const SfEigItem *items, int first, int count, int n_max, int B,
                                       const int32_t *vis, const float2 *factors, const __half2 *weights,
                                       const int32_t *fixed_counts, int k_rule, float delta, int shrink,
-                                      float *evals, int32_t *counts, float2 *weff, int num_sms,
+                                      float *evals, int32_t *counts, float2 *weff, uint32_t *status, int num_sms,
                                       cudaStream_t stream);
 cudaError_t sf_launch_eig_small(const sf_plan *p, const int32_t *vis, int k_rule, float delta, int shrink,
                                 float *evals, int32_t *counts, const int32_t *list, const int32_t *list_count,
