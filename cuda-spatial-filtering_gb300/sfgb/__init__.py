@@ -24,6 +24,12 @@ LIB_PATH = PKG / "libsfgb.so"
 HEADER = PKG.parent.parent / "include" / "sf_capi.h"
 
 SF_OK = 0
+# sf_status codes
+SF_ERR_INVALID_ARGUMENT = 1
+SF_ERR_UNSUPPORTED = 2
+SF_ERR_CUDA = 3
+SF_ERR_DEVICE = 4
+SF_ERR_NO_DEVICE = 5
 SF_WINDOW_PACKET = 0
 SF_WINDOW_ALIGNED = 1
 SF_EIG_ALL_BLOCKS = 0

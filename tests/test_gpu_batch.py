@@ -139,3 +139,32 @@ def test_batch_rejects_unsupported_shapes():
     with pytest.raises(sfgb.SfError) as ei:
         sfgb.Batch([16], 500, 4)  # T not a multiple of 128
     assert ei.value.code == 2
+
+
+def test_batch_k_beyond_kept_eigenvectors_is_clamped_and_reported():
+    """A 128-receiver unit keeps 32 eigenvectors of its tridiagonal: a fixed K
+    of 40 nulls the top 32, returns K = 32 and raises the bad-shape bit; a
+    36-receiver unit in the same batch takes its K of 20 in full."""
+    recv = [128, 36]
+    fixed = np.array([40, 20], np.int32)
+    xs, ws = orc.synth_batch(recv, 512, 4, seed=11)
+    bt = sfgb.Batch(recv, 512, 4)
+    bt.set_weights(bt.pack_weights(ws))
+    bt.set_fixed_counts(fixed)
+    s = torch.as_tensor(bt.pack_samples(xs)).cuda()
+    vis = torch.empty(bt.totals["vis"], dtype=torch.int32, device="cuda")
+    ev = torch.empty(bt.totals["evals"], dtype=torch.float32, device="cuda")
+    cnt = torch.full((bt.n_units, 2), -1, dtype=torch.int32, device="cuda")
+    beams = torch.empty(2 * bt.totals["beams"], dtype=torch.float16, device="cuda")
+    bt.run(s, sfgb.SF_K_FIXED, 0.0, False, vis, ev, cnt, beams)
+    torch.cuda.synchronize()
+    rc, bits = bt.status()
+    assert rc == sfgb.SF_ERR_DEVICE and bits & sfgb.SF_DEV_BAD_SHAPE
+    c = cnt.cpu().numpy()
+    assert np.array_equal(c[0], [32, 32]) and np.array_equal(c[1], [20, 20])
+    # the 36-receiver unit's result is still the oracle's
+    ref = orc.unit_chain(xs[1], ws[1], "fixed", k_fixed=20)
+    e = bt.unit_evals(ev.cpu().numpy(), 1)
+    assert np.all(np.abs(e - ref["evals"]) <= 2e-5 * np.abs(ref["evals"]).max(axis=-1, keepdims=True))
+    assert np.all(np.isfinite(beams.cpu().numpy().astype(np.float32)))
+    bt.close()
