@@ -511,8 +511,11 @@ __device__ __forceinline__ void eig_small_one(const SmallEigArgs &a, const Small
   __syncthreads();
   {
     const int ne = need_all ? n : Kfix;
-    int g = 1;  // threads per eigenvalue: a power of two, so a group lies in one warp
-    while (g < 32 && 2 * g * ne <= NT) g *= 2;
+    // threads per eigenvalue: a power of two, so a group lies in one warp; at most 128 threads in
+    // all (the passes are issue-bound beyond four warps: 16 warps on 128 eigenvalues measured 3x
+    // the cycles of 4)
+    int g = 1;
+    while (g < 32 && 2 * g * ne <= (NT < 128 ? NT : 128)) g *= 2;
     const int r = tid / g, sub = tid - r * g;
     const bool mine = r < ne;
     const int j = need_all ? r : n - 1 - r;
