@@ -168,3 +168,12 @@ def test_batch_k_beyond_kept_eigenvectors_is_clamped_and_reported():
     assert np.all(np.abs(e - ref["evals"]) <= 2e-5 * np.abs(ref["evals"]).max(axis=-1, keepdims=True))
     assert np.all(np.isfinite(beams.cpu().numpy().astype(np.float32)))
     bt.close()
+
+
+def test_batch_sizes_between_64_and_128_receivers():
+    """Units of 68, 100 and 124 receivers (the sixteen-warp eigensolver with
+    partly filled lanes and row slots) beside 4 and 60, against the oracle."""
+    recv = [68, 100, 124, 4, 60, 100]
+    out = _run(recv, 512, 6, seed=13, k_rule=sfgb.SF_K_NOISE_FLOOR, delta=10.0)
+    _check(out, recv, 6, sfgb.SF_K_NOISE_FLOOR, 10.0)
+    out["batch"].close()
