@@ -152,3 +152,26 @@ def _noalloc_with_delays(sh, samples, scales, weights, delays):
                               fixed_counts=fx, counts=cnt, status=status)
     torch.cuda.synchronize()
     return beams.cpu().numpy().astype(np.float32), cnt.cpu().numpy(), int(status.item())
+
+
+def test_noalloc_status_word_is_only_or_ed():
+    # The caller's status word is only OR-ed into, never cleared: a bit left from
+    # an earlier call stays set after a clean call, and the results are unchanged.
+    sh, samples, scales, weights, gains, delays, fixed = _inputs(5)
+    s = torch.as_tensor(samples).cuda()
+    sc = torch.as_tensor(scales).cuda()
+    w = torch.as_tensor(np.ascontiguousarray(weights)).cuda()
+    fac = torch.as_tensor(np.ascontiguousarray(np.stack([gains.real, gains.imag], -1).astype(np.float32))).cuda()
+    dl = torch.as_tensor(delays).cuda()
+    fx = torch.as_tensor(fixed).cuda()
+    beams = torch.full((sh.C, 2, 2 * sh.B, sh.T, 2), float("nan"), dtype=torch.float16, device="cuda")
+    cnt = torch.full((sh.C, 2), -1, dtype=torch.int32, device="cuda")
+    stale = sfgb.SF_DEV_BAD_DELAY
+    status = torch.full((1,), stale, dtype=torch.int32, device="cuda")
+    sfgb.run_adaptive_noalloc(SHAPE, s, sc, w, sfgb.SF_K_FIXED, 0.0, False, beams, factors=fac, delays=dl,
+                              fixed_counts=fx, counts=cnt, status=status)
+    torch.cuda.synchronize()
+    assert int(status.item()) == stale
+    ref_beams, ref_counts = _plan_path(sh, samples, scales, weights, gains, delays, fixed, sfgb.SF_K_FIXED, 0.0)
+    assert np.array_equal(cnt.cpu().numpy(), ref_counts)
+    assert _close(beams.cpu().numpy().astype(np.float32), ref_beams)
