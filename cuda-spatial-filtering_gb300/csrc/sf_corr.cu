@@ -210,13 +210,6 @@ __device__ __forceinline__ void convert_word(uint32_t word, uint32_t scw, __half
   p1 = x23;
 }
 
-__device__ __forceinline__ void emit_vis(const CorrArgs &a, int c, int p, int i, int q, int j,
-                                         int comp, int val, bool whole) {
-  const size_t idx = ((((size_t)c * a.NBL + baseline_of(i, j)) * 2 + p) * 2 + q) * 2 + comp;
-  if (whole) a.vis[idx] = val;
-  else atomicAdd(a.vis + idx, val);  // exact: integer addition in any order
-}
-
 // Shared-memory descriptor with explicit strides (128-byte swizzle).  K-major:
 // lbo unused, sbo = 8-row group stride.  MN-major: lbo = stride between
 // 64-value MN atoms, sbo = stride between 8-row K groups.
@@ -503,6 +496,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
         const bool first = kb - 2 * pb < CHUNK_KBLK;  // the item's first chunk
         const bool last = kb == 2 * pe - 1;           // the item's last chunk
         const uint32_t tacc = tmem + abuf * a.acc_stride;
+        // the channel's visibilities: (i, j, p, q, comp) at 8 (j (j + 1) / 2 + i) + 4 p + 2 q + comp
+        int32_t *const vis_c = a.vis + (size_t)c * a.NBL * 8;
+        const bool whole = last && *reinterpret_cast<volatile int *>(&h.items[it].w) != 0;
         for (int cb = 0; cb < ncols / 16; ++cb) {
           uint32_t fv[16], sv[16];
           tmem_ld16(tacc + cb * 16, fv);
@@ -529,21 +525,23 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
           const int i = k >> 1;
           const bool row_ok = ok && u < R4;
           const int m0 = main_region ? cb * 8 : 64 + ((cb * 16 - NR) >> 1);
-          const bool whole = *reinterpret_cast<volatile int *>(&h.items[it].w) != 0;
+          const int lane_off = 8 * i + 4 * p + comp;
+          // Column pair m = 2 j + q is warp-uniform, so each store's address is
+          // the lane's row offset plus a constant (a per-element index chain
+          // made this write-out, not the tensor work, the kernel's tail).
+          // Every i <= j lies in a main-tile row (i < 32) or in the corner
+          // (i, j >= 32).
 #pragma unroll
           for (int e2 = 0; e2 < 8; ++e2) {
-            const int g0 = acc[2 * e2];
-            const int g1 = acc[2 * e2 + 1];
-            const int other = __shfl_xor_sync(0xffffffffu, g1, 1);
-            const int val = comp ? g0 - other : g0 + other;
+            const int other = __shfl_xor_sync(0xffffffffu, acc[2 * e2 + 1], 1);
+            const int val = comp ? acc[2 * e2] - other : acc[2 * e2] + other;
             const int m = m0 + e2;
-            if (!row_ok || 2 * m >= R4) continue;
-            const int q = m & 1;
             const int j = m >> 1;
-            if (i <= j) emit_vis(a, c, p, i, q, j, comp, val, whole);
-            // Rows m >= 64 are not main-tile rows: their entries with a main-tile
-            // column come from here, conjugated.
-            if (main_region && m >= 64 && j <= i) emit_vis(a, c, q, j, p, i, comp, comp ? -val : val, whole);
+            if (row_ok && 2 * m < R4 && i <= j) {
+              int32_t *dst = vis_c + (4 * j * (j + 1) + 2 * (m & 1) + lane_off);
+              if (whole) *dst = val;
+              else atomicAdd(dst, val);  // exact: integer addition in any order
+            }
           }
         }
         if (!last) tmem_wait_st();
