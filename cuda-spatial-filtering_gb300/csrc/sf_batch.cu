@@ -383,6 +383,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_batch_kernel(const __grid_cons
         const int u = it.row0 + row;
         const int k = u >> 1, comp = u & 1, p = k & 1, i = k >> 1;
         const bool row_ok = ok && u < 4 * R;
+        // (i, j, p, q, comp) sits at 8 (j (j + 1) / 2 + i) + 4 p + 2 q + comp of
+        // the unit's visibilities; column pair m = 2 j + q is warp-uniform
+        int32_t *const vis_u = a.vis + un.vis_off;
+        const int lane_off = 8 * i + 4 * p + comp;
         for (int cb = 0; cb < it.n / 16; ++cb) {
           uint32_t fv[16], sv[16];
           tmem_ld16(tq + buf * ACC_STRIDE + cb * 16, fv);
@@ -402,14 +406,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_batch_kernel(const __grid_cons
           // final chunk: combine (re, im) row pairs and store the packed upper triangle
 #pragma unroll
           for (int e2 = 0; e2 < 8; ++e2) {
-            const int g0 = acc[2 * e2];
             const int other = __shfl_xor_sync(0xffffffffu, acc[2 * e2 + 1], 1);
-            const int val = comp ? g0 - other : g0 + other;
+            const int val = comp ? acc[2 * e2] - other : acc[2 * e2] + other;
             const int m = (it.c0 >> 1) + cb * 8 + e2;
-            if (!row_ok || 2 * m >= 4 * R) continue;
-            const int q = m & 1, j = m >> 1;
-            if (i <= j)
-              a.vis[un.vis_off + ((static_cast<long long>(baseline_of(i, j)) * 2 + p) * 2 + q) * 2 + comp] = val;
+            const int j = m >> 1;
+            if (row_ok && 2 * m < 4 * R && i <= j) vis_u[4 * j * (j + 1) + 2 * (m & 1) + lane_off] = val;
           }
         }
         if (!last_chunk) tmem_wait_st();
