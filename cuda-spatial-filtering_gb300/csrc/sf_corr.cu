@@ -658,33 +658,41 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
         failed |= !ok;
         if (ok) {
           uint8_t *wt = w_ptr + wb * a.wtile_bytes;
-          const int nchunk = a.katoms * 8;  // 16-byte chunks per row
-          for (int task = ct; task < a.BN * nchunk; task += NUM_CONV_THREADS) {
-            const int n = task / nchunk;
-            const int ch = task - n * nchunk;
-            const int atom = ch >> 3, cc = ch & 7;
-            const int pn = n / (2 * a.NB);
-            const int mn = (n >> 1) - pn * a.NB;
-            const int cn = n & 1;
-            uint32_t pk[4];
+          // Only entries with the output's pol (pu == pn) and a real receiver
+          // are nonzero; the rest of both tiles was zeroed at start and is
+          // never written.  Weight w = weff[c][pn][mn][r] fills rows
+          // n = 2 (pn NB + mn) + cn at columns u = 4 r + 2 pn + cu with
+          // (w.x, -w.y) for cn = 0 and (w.y, w.x) for cn = 1.  Each thread
+          // loads all its weights before storing any, so a channel's tile costs
+          // one memory latency instead of one per 16-byte chunk (the serial
+          // form was ~9 k cycles per channel between the stage loops).
+          constexpr int MAXW = (2 * MAX_BEAM_OUT * MAX_R + NUM_CONV_THREADS - 1) / NUM_CONV_THREADS;
+          const int nw = 2 * a.NB * R;
+          float2 wv[MAXW];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              float vals[2];
-#pragma unroll
-              for (int dd = 0; dd < 2; ++dd) {
-                const int u = atom * 64 + cc * 8 + q * 2 + dd;
-                const int r = u >> 2, pu = (u >> 1) & 1, cu = u & 1;
-                float v = 0.0f;
-                if (pn < 2 && u < 4 * R && pu == pn) {
-                  const float2 w = a.weff[(((size_t)c * 2 + pn) * a.NBW + mn) * R + r];
-                  v = cn == 0 ? (cu == 0 ? w.x : -w.y) : (cu == 0 ? w.y : w.x);
-                }
-                vals[dd] = v;
-              }
-              pk[q] = u32_of(__floats2half2_rn(vals[0], vals[1]));
+          for (int k = 0; k < MAXW; ++k) {
+            const int idx = ct + k * NUM_CONV_THREADS;
+            if (idx < nw) {
+              const int q = idx / R, r = idx - q * R;  // q = pn NB + mn
+              const int pn = q / a.NB, mn = q - pn * a.NB;
+              wv[k] = a.weff[(((size_t)c * 2 + pn) * a.NBW + mn) * R + r];
             }
-            *reinterpret_cast<uint4 *>(wt + atom * (a.BN * 128) + n * 128 + ((cc ^ (n & 7)) << 4)) =
-                make_uint4(pk[0], pk[1], pk[2], pk[3]);
+          }
+#pragma unroll
+          for (int k = 0; k < MAXW; ++k) {
+            const int idx = ct + k * NUM_CONV_THREADS;
+            if (idx < nw) {
+              const int q = idx / R, r = idx - q * R;
+              const int pn = q / a.NB;
+              const int n0 = 2 * q;
+              const int u = 4 * r + 2 * pn;
+              const int kk = u & 63, cc = kk >> 3;
+              uint8_t *blk = wt + (u >> 6) * (a.BN * 128) + ((kk & 7) << 1);
+              *reinterpret_cast<uint32_t *>(blk + n0 * 128 + ((cc ^ (n0 & 7)) << 4)) =
+                  u32_of(__floats2half2_rn(wv[k].x, -wv[k].y));
+              *reinterpret_cast<uint32_t *>(blk + (n0 + 1) * 128 + ((cc ^ ((n0 + 1) & 7)) << 4)) =
+                  u32_of(__floats2half2_rn(wv[k].y, wv[k].x));
+            }
           }
         }
         fence_proxy_async_smem();
