@@ -575,3 +575,37 @@ def test_shallow_packet_ring_corr_beam_split_channels():
     ref = orc.corr_beam_chain(sh, samples, scales, weights)
     assert np.array_equal(vis.cpu().numpy(), ref["vis"])
     _beam_close(beams.cpu().numpy().astype(np.float32), ref["beams"], sh.B)
+
+
+# --------------------------------------------------------------------------
+# Odd receiver and beam counts: the beamformer's weight tile is built from
+# its nonzero entries only (rows 2 (p NB + b) + {0, 1}, columns 4 r + 2 p +
+# {0, 1}); rows past 4 NB and columns past 4 R stay the zeros written at
+# kernel start.  R = 13 (one FPGA) and R = 45 (five FPGAs, 10 beams per pol
+# over two slots: 40 of 48 tile rows).
+# --------------------------------------------------------------------------
+@pytest.mark.parametrize("shape", [(24, 1, 16, 13, 13, 16, 3), (40, 5, 16, 45, 9, 16, 5)])
+def test_odd_receiver_and_beam_counts(shape):
+    sh = orc.Shape(*shape)
+    samples, scales, _ = orc.synth_inputs(sh, seed=51, n_interferers=1, frac_channels=0.5)
+    weights = orc.synth_weights(sh, seed=52)
+    # fused corr + beam (one slot)
+    plan = sfgb.Plan(sh.C, sh.F, sh.Tp, sh.R, sh.Rpp, sh.P, sh.B)
+    plan.set_weights(weights)
+    s, sc = _dev(samples, torch.int8), _dev(scales, torch.int16)
+    vis = torch.full(plan.vis_shape(), -7, dtype=torch.int32, device="cuda")
+    beams = torch.empty(plan.beams_shape(1), dtype=torch.float16, device="cuda")
+    plan.run_corr_beam(s, sc, vis, beams)
+    torch.cuda.synchronize()
+    rc, bits = plan.status()
+    assert rc == 0 and bits == 0
+    plan.close()
+    ref = orc.corr_beam_chain(sh, samples, scales, weights)
+    assert np.array_equal(vis.cpu().numpy(), ref["vis"])
+    _beam_close(beams.cpu().numpy().astype(np.float32), ref["beams"], sh.B)
+    # adaptive chain: beams of both slots from the eigensolver's effective weights
+    fixed = np.full(sh.C, 1)
+    got = _run_adaptive_gpu(sh, samples, scales, weights, sfgb.SF_K_FIXED, 0.0, fixed=fixed, want_evecs=False)
+    ref = orc.adaptive_chain(sh, samples, scales, weights, k_fixed=fixed)
+    assert np.array_equal(got["vis"], ref["vis"])
+    _beam_close(got["beams"], ref["beams"], sh.B)
