@@ -47,7 +47,9 @@
 //                    operand stage ahead; another hands each written stage to
 //                    the MMA issuer and returns its packets to the producer.
 // Operand stages: three when they fit beside a packet ring deep enough to
-// prefetch a stage (the correlator), else two (the beamformer's weight tiles).
+// prefetch a stage (the correlator; the beamformer alone when its last K atom
+// holds at most 16 values, stored compact as 32-byte rows with the 32-byte
+// swizzle in the operand and weight tiles), else two.
 // Every wait is bounded (about a second) and reports through the status word.
 #include <algorithm>
 #include <cstdio>
@@ -106,6 +108,9 @@ struct CorrArgs {
   int BN;           // beam MMA N = round_up(4 NB, 16)
   int katoms;       // 64-column K atoms of the weight tile: ceil(NR / 64)
   uint32_t wtile_bytes;
+  uint32_t stage_bytes;  // one operand stage (natoms full atoms, or two + the compact last atom)
+  int compact;  // beamformer alone with 128 < NR <= 144: the last K atom holds its 16 values as
+                // 32-byte rows (32-byte swizzle) in the operand tile and the weight tile
   uint32_t tmem_cols, i32_off, beam_off;
   int nacc;  // fp32 chunk accumulators in tensor memory (2 = double-buffered)
   uint32_t acc_stride;  // tensor-memory columns between the fp32 accumulators
@@ -223,6 +228,18 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t addr, uint32_t lbo, uint
   return d;
 }
 
+// K-major, 32-byte swizzle: rows of 16 fp16 values (one K16 step), 8-row groups
+// 256 bytes apart.  Used for the compact last K atom of the beamformer.
+__device__ __forceinline__ uint64_t desc_sw32(uint32_t addr) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((addr >> 4) & 0x3FFFu);
+  d |= static_cast<uint64_t>(1u) << 16;          // lbo 16 bytes (unused: one atom along K)
+  d |= static_cast<uint64_t>(256u >> 4) << 32;   // sbo
+  d |= static_cast<uint64_t>(1u) << 46;
+  d |= static_cast<uint64_t>(6u) << 61;
+  return d;
+}
+
 // tcgen05.mma issue is serialised with the issuing thread's own instruction
 // stream, so the issue loops below are straight-line: no branch between MMAs.
 template <bool DO_CORR, bool DO_BEAM, bool CORNER>
@@ -236,7 +253,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
   const uint32_t sbase = smem_u32(smem);
   const uint32_t op_addr = (sbase + HEADER_BYTES + 1023u) & ~1023u;
   uint8_t *op_ptr = smem + (op_addr - sbase);
-  const uint32_t stage_bytes = static_cast<uint32_t>(a.natoms) * ATOM_BYTES;
+  const uint32_t stage_bytes = a.stage_bytes;
   const uint32_t SO = static_cast<uint32_t>(a.nstages);
   const uint32_t w_addr = op_addr + SO * stage_bytes;  // weight tiles (1024-aligned)
   uint8_t *w_ptr = op_ptr + SO * stage_bytes;
@@ -420,11 +437,16 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
               const uint64_t ad0 = d_k0 + (soff >> 4);
               const uint64_t bd0 = d_w0 + (woff >> 4);
               const uint32_t batom = (a.BN * 128) >> 4;
+              // the compact last K atom (K step 8): its own 32-byte-swizzle descriptors
+              const uint64_t ad2 = desc_sw32(op_addr + 2 * ATOM_BYTES + soff);
+              const uint64_t bd2 = desc_sw32(w_addr + woff + 2 * a.BN * 128);
 #pragma unroll
               for (int ks = 0; ks < MAX_R / 4; ++ks) {
                 const uint32_t kof = ((ks & 3) * 32) >> 4;
-                umma_f16_if(d, ad0 + ((ks >> 2) * (ATOM_BYTES >> 4) + kof), bd0 + ((ks >> 2) * batom + kof),
-                            idesc_beam, ks > 0 ? 1u : 0u, (ok && ks < nks) ? 1u : 0u);
+                const bool c2 = ks == 8 && a.compact;
+                umma_f16_if(d, c2 ? ad2 : ad0 + ((ks >> 2) * (ATOM_BYTES >> 4) + kof),
+                            c2 ? bd2 : bd0 + ((ks >> 2) * batom + kof), idesc_beam, ks > 0 ? 1u : 0u,
+                            (ok && ks < nks) ? 1u : 0u);
               }
             }
             umma_commit(&h.beam_full[beam_iter & 1u]);
@@ -582,6 +604,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
     int woff0[MAX_JP];                   // window offset of the pair's first receiver
     uint32_t roff0[MAX_JP], dr1[MAX_JP]; // word offset in a slot; second receiver's word - first's
     uint32_t stoff[MAX_JP];              // this lane's 16-byte chunk in group 0 of a stage
+    uint32_t gstr[MAX_JP];               // bytes between the 32-sample groups of that atom
     bool same[MAX_JP], has1[MAX_JP];
     int woff1[MAX_JP];
 #pragma unroll
@@ -594,7 +617,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
       dr1[k] = static_cast<uint32_t>(h.rx_off[r1] - h.rx_off[r0]);
       same[k] = woff1[k] == woff0[k];
       has1[k] = 2 * jp + 1 < R;
-      stoff[k] = (jp >> 3) * ATOM_BYTES + lane * 128 + (((jp & 7) ^ (lane & 7)) << 4);
+      // rows of 128 bytes (128-byte swizzle), or of 32 bytes in the compact last
+      // atom (32-byte swizzle: the chunk flips with bit 2 of the sample)
+      const bool cpt = a.compact && (jp >> 3) == 2;
+      stoff[k] = cpt ? 2 * ATOM_BYTES + lane * 32 + (((jp & 1) ^ ((lane >> 2) & 1)) << 4)
+                     : (jp >> 3) * ATOM_BYTES + lane * 128 + (((jp & 7) ^ (lane & 7)) << 4);
+      gstr[k] = cpt ? 32 * 32 : 32 * 128;
     }
     uint32_t unit_bits = 0;  // leader: bit s = ring slot s holds a packet whose scales are all 1
     int q_rel = 0;           // hand-off warp: first packet not yet returned to the producer
@@ -688,10 +716,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
               const int u = 4 * r + 2 * pn;
               const int kk = u & 63, cc = kk >> 3;
               uint8_t *blk = wt + (u >> 6) * (a.BN * 128) + ((kk & 7) << 1);
-              *reinterpret_cast<uint32_t *>(blk + n0 * 128 + ((cc ^ (n0 & 7)) << 4)) =
-                  u32_of(__floats2half2_rn(wv[k].x, -wv[k].y));
-              *reinterpret_cast<uint32_t *>(blk + (n0 + 1) * 128 + ((cc ^ ((n0 + 1) & 7)) << 4)) =
-                  u32_of(__floats2half2_rn(wv[k].y, wv[k].x));
+              // 128-byte rows, or 32-byte rows in the compact last atom
+              const bool cpt = a.compact && (u >> 6) == 2;
+              const int n1 = n0 + 1;
+              const uint32_t o0 = cpt ? n0 * 32 + (((cc & 1) ^ ((n0 >> 2) & 1)) << 4) : n0 * 128 + ((cc ^ (n0 & 7)) << 4);
+              const uint32_t o1 = cpt ? n1 * 32 + (((cc & 1) ^ ((n1 >> 2) & 1)) << 4) : n1 * 128 + ((cc ^ (n1 & 7)) << 4);
+              *reinterpret_cast<uint32_t *>(blk + o0) = u32_of(__floats2half2_rn(wv[k].x, -wv[k].y));
+              *reinterpret_cast<uint32_t *>(blk + o1) = u32_of(__floats2half2_rn(wv[k].y, wv[k].x));
             }
           }
         }
@@ -763,7 +794,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
                   }
                   o[e] = u32_of(__floats2half2_rn(xr, xi));  // fp16(x * scale)
                 }
-                sts128(stage_s + stoff[k] + g * (32 * 128), o[0], o[1], o[2], o[3]);
+                sts128(stage_s + stoff[k] + g * gstr[k], o[0], o[1], o[2], o[3]);
               }
             }
           } else if (ok && stage_fast && off_min == off_max) {
@@ -800,7 +831,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
                   o[2 * e] = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4140)), bias));
                   o[2 * e + 1] = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4342)), bias));
                 }
-                sts128(stage_s + stoff[k] + g * (32 * 128), o[0], o[1], o[2], o[3]);
+                sts128(stage_s + stoff[k] + g * gstr[k], o[0], o[1], o[2], o[3]);
               }
             }
           } else if (ok && stage_fast) {
@@ -837,7 +868,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
                   o[2 * e] = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4140)), bias));
                   o[2 * e + 1] = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4342)), bias));
                 }
-                sts128(stage_s + stoff[k] + g * (32 * 128), o[0], o[1], o[2], o[3]);
+                sts128(stage_s + stoff[k] + g * gstr[k], o[0], o[1], o[2], o[3]);
               }
             }
           } else if (ok) {
@@ -882,7 +913,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
                     o[2 * e] = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4140)), bias));
                     o[2 * e + 1] = u32_of(__hsub2(h2_of(__byte_perm(biased, 0x64646464u, 0x4342)), bias));
                   }
-                  sts128(stage_s + stoff[k] + g * (32 * 128), o[0], o[1], o[2], o[3]);
+                  sts128(stage_s + stoff[k] + g * gstr[k], o[0], o[1], o[2], o[3]);
                 }
               } else {
                 const int r0 = 2 * jp;
@@ -895,7 +926,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) sf_corrbeam_kernel(const CorrArgs
                   __half2 a0, a1, b0, b1;
                   convert_word(wd[g][0], sc0, a0, a1);
                   convert_word(wd[g][1], sc1, b0, b1);
-                  sts128(stage_s + stoff[k] + g * (32 * 128), u32_of(a0), u32_of(a1), u32_of(b0), u32_of(b1));
+                  sts128(stage_s + stoff[k] + g * gstr[k], u32_of(a0), u32_of(a1), u32_of(b0), u32_of(b1));
                 }
               }
             }
@@ -1013,7 +1044,14 @@ cudaError_t sf_launch_corrbeam(const sf_plan *p, const int8_t *samples, const in
   a.NBW = 2 * p->B;
   a.BN = ((4 * n_beams_out + 15) / 16) * 16;
   a.katoms = (a.NR + 63) / 64;
-  a.wtile_bytes = do_beam ? static_cast<uint32_t>(a.katoms * a.BN * 128) : 0u;
+  // The beamformer alone reads the tile K-major only, so a last K atom with at
+  // most 16 values can be stored as 32-byte rows: 36 instead of 48 KB per
+  // operand stage at R = 36, which leaves room for a third operand stage.
+  a.compact = (!do_corr && do_beam && a.NR > 128 && a.NR <= 144) ? 1 : 0;
+  a.stage_bytes = a.compact ? 2 * ATOM_BYTES + TILE_T * 32 : static_cast<uint32_t>(a.natoms) * ATOM_BYTES;
+  a.wtile_bytes = do_beam ? (a.compact ? ((2 * a.BN * 128 + a.BN * 32 + 1023u) & ~1023u)
+                                       : static_cast<uint32_t>(a.katoms * a.BN * 128))
+                          : 0u;
   const int ncols = a.NR + (a.NR > 128 ? a.NR - 128 : 0);
   a.nacc = 1;
   a.acc_stride = ncols;
@@ -1043,7 +1081,7 @@ cudaError_t sf_launch_corrbeam(const sf_plan *p, const int8_t *samples, const in
   const int prefetch_slots = (2 * TILE_T - 1) / p->Tp + 5;
   // ring depth beside `stages` operand stages (a power of two)
   auto ring_depth = [&](int stages) {
-    const long fixed = HEADER_BYTES + 1024 + (long)stages * a.natoms * ATOM_BYTES + 2 * (long)a.wtile_bytes;
+    const long fixed = HEADER_BYTES + 1024 + (long)stages * a.stage_bytes + 2 * (long)a.wtile_bytes;
     const long avail = (long)max_smem - fixed;
     int ns = avail > 0 ? (int)std::min<long>(MAX_SLOTS, avail / a.slot_stride) : 0;
     while (ns & (ns - 1)) ns &= ns - 1;  // round down to a power of two
@@ -1055,7 +1093,7 @@ cudaError_t sf_launch_corrbeam(const sf_plan *p, const int8_t *samples, const in
   if (ns < need_slots) return cudaErrorInvalidConfiguration;
   a.num_slots = ns;
   a.prefetch = ns >= prefetch_slots ? 1 : 0;
-  const size_t smem = HEADER_BYTES + 1024 + (size_t)a.nstages * a.natoms * ATOM_BYTES + 2 * (size_t)a.wtile_bytes +
+  const size_t smem = HEADER_BYTES + 1024 + (size_t)a.nstages * a.stage_bytes + 2 * (size_t)a.wtile_bytes +
                       (size_t)ns * a.slot_stride;
   const int grid = std::max(1, std::min(p->C, p->num_sms));
   // WorkItems computes (tail stages) x (CTA index) in 32 bits; a CTA holds at

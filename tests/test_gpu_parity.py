@@ -581,10 +581,12 @@ def test_shallow_packet_ring_corr_beam_split_channels():
 # Odd receiver and beam counts: the beamformer's weight tile is built from
 # its nonzero entries only (rows 2 (p NB + b) + {0, 1}, columns 4 r + 2 p +
 # {0, 1}); rows past 4 NB and columns past 4 R stay the zeros written at
-# kernel start.  R = 13 (one FPGA) and R = 45 (five FPGAs, 10 beams per pol
-# over two slots: 40 of 48 tile rows).
+# kernel start.  R = 13 (one FPGA), R = 34 (the beamformer's compact last K
+# atom with 8 of its 16 values padding) and R = 45 (five FPGAs, 10 beams per
+# pol over two slots: 40 of 48 tile rows).
 # --------------------------------------------------------------------------
-@pytest.mark.parametrize("shape", [(24, 1, 16, 13, 13, 16, 3), (40, 5, 16, 45, 9, 16, 5)])
+@pytest.mark.parametrize("shape", [(24, 1, 16, 13, 13, 16, 3), (24, 2, 16, 34, 17, 16, 3),
+                                   (40, 5, 16, 45, 9, 16, 5)])
 def test_odd_receiver_and_beam_counts(shape):
     sh = orc.Shape(*shape)
     samples, scales, _ = orc.synth_inputs(sh, seed=51, n_interferers=1, frac_channels=0.5)
